@@ -1,0 +1,367 @@
+"""Python host API over libchrono_gpu.so, mirroring the reference's processor interface.
+
+    chrono-photo (Rust)                          this module
+    Threshold::abs/rel (src/options.rs:189-244)  Threshold
+    Fade (src/options.rs:60-139)                 Fade
+    OutlierProcessor::new/process (chrono.rs)    OutlierProcessor(...).process(frames)
+    SimpleProcessor::new/process (simple.rs)     SimpleProcessor(...).process(frames)
+    ShakeAnalyzer::analyze (shake.rs:190-313)    ShakeAnalyzer().analyze(frames, ...)
+    Crop::create (shake.rs:136-176)              Crop.create(offsets, width, height)
+
+Frames are numpy uint8 arrays [n, height, width, channels] (or a list of [h, w, c] arrays):
+the decoded images the reference reads through `image::open`. Every call runs on the GPU;
+there is no CPU path.
+"""
+import ctypes as ct
+
+import numpy as np
+
+from . import _abi
+from ._abi import ChronoError, lib
+
+
+def _check(ctx, rc, what=""):
+    if rc != _abi.CP_OK:
+        msg = what
+        if ctx is not None:
+            buf = ct.create_string_buffer(512)
+            lib().cp_ctx_last_error(ctx, buf, 512)
+            if buf.value:
+                msg = (what + ": " if what else "") + buf.value.decode()
+        raise ChronoError(rc, msg)
+
+
+class Threshold:
+    """`(abs|rel)/min[/max]`; max defaults to min as the reference's parser does."""
+
+    def __init__(self, absolute=True, min=0.05, max=None):
+        self.absolute = bool(absolute)
+        self.min = float(min)
+        self.max = float(min if max is None else max)
+
+    @classmethod
+    def abs(cls, mn, mx=None):
+        return cls(True, mn, mx)
+
+    @classmethod
+    def rel(cls, mn, mx=None):
+        return cls(False, mn, mx)
+
+    @classmethod
+    def parse(cls, s):
+        parts = s.split("/")
+        if parts[0] not in ("abs", "absolute", "rel", "relative") or len(parts) < 2:
+            raise ValueError("threshold must be (abs|rel)/min[/max]: %r" % s)
+        return cls(parts[0].startswith("abs"), float(parts[1]),
+                   float(parts[2]) if len(parts) > 2 else None)
+
+
+class Fade:
+    """`(clamp|repeat)/(abs|rel)/f,v/...`; Fade.none() is the default (all 1)."""
+
+    def __init__(self, repeat=False, absolute=True, points=()):
+        self.repeat = bool(repeat)
+        self.absolute = bool(absolute)
+        self.points = [(int(f), float(v)) for f, v in points]
+        self.enabled = len(self.points) > 0
+
+    @classmethod
+    def none(cls):
+        return cls()
+
+    @classmethod
+    def parse(cls, s):
+        parts = s.split("/")
+        if parts[0] not in ("clamp", "repeat") or parts[1] not in ("abs", "absolute", "rel", "relative"):
+            raise ValueError("fade must be (clamp|repeat)/(abs|rel)/f,v/...: %r" % s)
+        pts = []
+        for p in parts[2:]:
+            f, v = p.split(",")
+            pts.append((int(f), float(v)))
+        return cls(parts[0] == "repeat", parts[1].startswith("abs"), pts)
+
+    def to_c(self, keep):
+        f = _abi.Fade()
+        f.enabled = 1 if self.enabled else 0
+        f.repeat = 1 if self.repeat else 0
+        f.absolute = 1 if self.absolute else 0
+        f.n_points = len(self.points)
+        if self.enabled:
+            fr = (ct.c_int32 * len(self.points))(*[p[0] for p in self.points])
+            va = (ct.c_float * len(self.points))(*[p[1] for p in self.points])
+            keep += [fr, va]
+            f.frames = ct.cast(fr, ct.POINTER(ct.c_int32))
+            f.values = ct.cast(va, ct.POINTER(ct.c_float))
+        return f
+
+    def lut(self, n, frame_offset=0):
+        """fade(i, n, frame_offset) for every sample i (src/chrono.rs:496-502)."""
+        keep = []
+        f = self.to_c(keep)
+        out = (ct.c_float * n)()
+        _check(None, lib().cp_fade_lut(ct.byref(f), n, frame_offset, out), "fade")
+        return np.frombuffer(out, dtype=np.float32).copy()
+
+
+def make_params(mode="outlier", threshold=None, outlier="extreme", background="random",
+                weights=(1.0, 1.0, 1.0, 1.0), fade=None, sample=None, seed=0x5EED, keep=None):
+    """cp_params from CLI-style values (defaults of src/cli.rs:192-216)."""
+    keep = keep if keep is not None else []
+    p = _abi.Params()
+    lib().cp_params_default(ct.byref(p))
+    threshold = threshold or Threshold.abs(0.05, 0.2)
+    if isinstance(threshold, str):
+        threshold = Threshold.parse(threshold)
+    p.mode = _abi.MODE[mode]
+    p.thr_abs = 1 if threshold.absolute else 0
+    p.thr_min = threshold.min
+    p.thr_max = threshold.max
+    p.outlier = _abi.OUTLIER[outlier]
+    p.background = _abi.BACKGROUND[background]
+    w = list(weights) + [1.0] * (4 - len(weights))
+    for i in range(4):
+        p.weights[i] = float(w[i])
+    if isinstance(fade, str):
+        fade = Fade.parse(fade)
+    p.fade = (fade or Fade.none()).to_c(keep)
+    if sample is not None and len(sample) > 0:
+        arr = (ct.c_int32 * len(sample))(*[int(s) for s in sample])
+        keep.append(arr)
+        p.sample = ct.cast(arr, ct.POINTER(ct.c_int32))
+        p.n_sample = len(sample)
+    p.rng_seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    return p
+
+
+def _as_stack(frames):
+    if isinstance(frames, np.ndarray):
+        a = np.ascontiguousarray(frames, dtype=np.uint8)
+        if a.ndim == 3:
+            a = a[..., None]
+        return a
+    return np.ascontiguousarray(np.stack([np.asarray(f, dtype=np.uint8) for f in frames]))
+
+
+class Context:
+    """One device context (cp_ctx): streams, device memory accounting, staging buffers."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        h = ct.c_void_p()
+        rc = lib().cp_ctx_create(device, hbm_budget, ct.byref(h))
+        _check(None, rc, "cp_ctx_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().cp_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc, what=""):
+        _check(self.handle, rc, what)
+
+    # ---- device memory ------------------------------------------------------------------
+    def alloc(self, nbytes):
+        p = ct.c_void_p()
+        self.check(lib().cp_dev_alloc(self.handle, nbytes, ct.byref(p)), "cp_dev_alloc")
+        return p.value
+
+    def free(self, ptr):
+        self.check(lib().cp_dev_free(self.handle, ptr), "cp_dev_free")
+
+    def upload(self, arr, ptr=None):
+        arr = np.ascontiguousarray(arr)
+        # 16 spare bytes: the kernels' 16-byte row copies may read past a frame's last pixel
+        ptr = ptr or self.alloc(arr.nbytes + 16)
+        self.check(lib().cp_memcpy_h2d(self.handle, ptr, arr.ctypes.data, arr.nbytes, None), "h2d")
+        return ptr
+
+    def download(self, ptr, shape, dtype=np.uint8):
+        out = np.empty(shape, dtype=dtype)
+        self.check(lib().cp_memcpy_d2h(self.handle, out.ctypes.data, ptr, out.nbytes, None), "d2h")
+        return out
+
+    def synchronize(self):
+        self.check(lib().cp_ctx_synchronize(self.handle), "synchronize")
+
+    # ---- compositing --------------------------------------------------------------------
+    def composite(self, frames, params=None, blend=True, debug=False, crop=None,
+                  src_size=None, frame_offset=0, **kw):
+        """Host-memory composite of one stack (cp_composite). Returns
+        (composite, blend_mask or None, warnings[, debug dict])."""
+        keep = []
+        p = params if params is not None else make_params(keep=keep, **kw)
+        a = _as_stack(frames)
+        n, h, w, c = a.shape
+        st = _abi.Stack()
+        st.n = n
+        st.channels = c
+        st.base = a.ctypes.data
+        st.frame_stride = h * w * c
+        st.frame_offset = frame_offset
+        if crop is not None:
+            cw, chh = src_size if src_size else (None, None)
+            ow, oh = crop[1]
+            origins = np.ascontiguousarray(np.asarray(crop[0], dtype=np.int32).reshape(-1))
+            keep.append(origins)
+            st.crop = origins.ctypes.data_as(ct.POINTER(ct.c_int32))
+            st.src_width, st.src_height = w, h
+            st.width, st.height = ow, oh
+            h, w = oh, ow
+        else:
+            st.width, st.height = w, h
+        out = np.empty((h, w, c), dtype=np.uint8)
+        bl = np.empty((h, w, c), dtype=np.uint8) if blend and p.mode == 0 else None
+        warn = ct.c_uint64(0)
+        dbg_arrays = None
+        dbg = None
+        if debug:
+            words = (n + 31) // 32
+            dbg_arrays = {
+                "median": np.zeros((h, w, c), np.float32),
+                "q1": np.zeros((h, w, c), np.float32),
+                "q3": np.zeros((h, w, c), np.float32),
+                "outlier_bits": np.zeros((h, w, words), np.uint32),
+                "chosen": np.zeros((h, w), np.int32),
+                "background": np.zeros((h, w), np.int32),
+                "n_outliers": np.zeros((h, w), np.int32),
+            }
+            dbg = _abi.Debug(*[dbg_arrays[k].ctypes.data for k in
+                               ("median", "q1", "q3", "outlier_bits", "chosen", "background",
+                                "n_outliers")])
+        rc = lib().cp_composite(self.handle, ct.byref(st), ct.byref(p), out.ctypes.data,
+                                bl.ctypes.data if bl is not None else None,
+                                ct.byref(dbg) if dbg is not None else None, ct.byref(warn))
+        self.check(rc, "cp_composite")
+        if debug:
+            return out, bl, warn.value, dbg_arrays
+        return out, bl, warn.value
+
+    def shake_analyze(self, frames, anchors, anchor_radius, search_radius, diffs=False):
+        """ShakeAnalyzer::analyze on the device: per-frame (dx, dy) offsets."""
+        a = _as_stack(frames)
+        n, h, w, c = a.shape
+        ptrs = []
+        try:
+            for i in range(n):
+                ptrs.append(self.upload(a[i]))
+            parr = (ct.c_void_p * n)(*ptrs)
+            anc = np.ascontiguousarray(np.asarray(anchors, dtype=np.int32).reshape(-1))
+            offs = np.zeros((n, 2), np.int32)
+            S = 2 * search_radius + 1
+            dd = np.zeros((max(n - 1, 0), S, S), np.int32) if diffs else None
+            rc = lib().cp_shake_analyze_device(
+                self.handle, parr, n, w, h, c, anc.ctypes.data_as(_abi.I32P), len(anc) // 2,
+                anchor_radius, search_radius, offs.ctypes.data_as(_abi.I32P),
+                dd.ctypes.data_as(_abi.I32P) if dd is not None else None)
+            self.check(rc, "cp_shake_analyze_device")
+        finally:
+            for q in ptrs:
+                self.free(q)
+        return (offs, dd) if diffs else offs
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context()
+    return _default_ctx
+
+
+class OutlierProcessor:
+    """OutlierProcessor::new (src/chrono.rs:46-71); process() composites one output frame."""
+
+    def __init__(self, threshold=None, background="random", outlier="extreme",
+                 weights=(1.0, 1.0, 1.0, 1.0), fade=None, sample=None, seed=0x5EED,
+                 context=None):
+        self.kw = dict(mode="outlier", threshold=threshold, background=background,
+                       outlier=outlier, weights=weights, fade=fade, sample=sample, seed=seed)
+        self.ctx = context
+
+    def process(self, frames, image_indices=None, debug=False):
+        """(composite, blend mask) like OutlierProcessor::process (src/chrono.rs:73-206)."""
+        ctx = self.ctx or default_context()
+        a = _as_stack(frames)
+        offset = 0
+        if image_indices is not None:
+            a = np.ascontiguousarray(a[list(image_indices)])
+            offset = int(image_indices[0])
+        r = ctx.composite(a, frame_offset=offset, debug=debug, **self.kw)
+        return r if debug else (r[0], r[1])
+
+
+class SimpleProcessor:
+    """SimpleProcessor::new (src/simple.rs:18-24): darker/lighter."""
+
+    def __init__(self, weights=(1.0, 1.0, 1.0, 1.0), fade=None, darker=True, context=None):
+        self.kw = dict(mode="darker" if darker else "lighter", weights=weights, fade=fade)
+        self.ctx = context
+
+    def process(self, frames, crop=None, image_indices=None):
+        ctx = self.ctx or default_context()
+        a = _as_stack(frames)
+        offset = 0
+        if image_indices is not None:
+            a = np.ascontiguousarray(a[list(image_indices)])
+            offset = int(image_indices[0])
+        return ctx.composite(a, frame_offset=offset, blend=False, crop=crop, **self.kw)[0]
+
+
+class Crop:
+    """Crop::create (src/shake.rs:136-176) via the library."""
+
+    @staticmethod
+    def create(offsets, width, height):
+        offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int32).reshape(-1))
+        n = len(offs) // 2
+        has = ct.c_int32(0)
+        crops = np.zeros((n, 4), np.int32)
+        _check(None, lib().cp_crop_create(offs.ctypes.data_as(_abi.I32P), n, width, height,
+                                          ct.byref(has), crops.ctypes.data_as(_abi.I32P)),
+               "cp_crop_create")
+        return crops if has.value else None
+
+
+class ShakeAnalyzer:
+    def __init__(self, context=None):
+        self.ctx = context
+
+    def analyze(self, frames, anchors, anchor_radius, search_radius):
+        ctx = self.ctx or default_context()
+        return [tuple(o) for o in ctx.shake_analyze(frames, anchors, anchor_radius, search_radius)]
+
+
+def video_windows(image_count, video_in, video_out=(None, None, 1)):
+    """chrono-video windows of src/main.rs:230-286: list of (output frame, indices)."""
+    (a, b, s), (c, d, t) = video_in, video_out
+    nw = ct.c_int32()
+    ni = ct.c_int64()
+    args = [image_count, a is not None, a or 0, b is not None, b or 0, s or 1,
+            c is not None, c or 0, d is not None, d or 0, t or 1]
+    _check(None, lib().cp_video_windows(*args, ct.byref(nw), ct.byref(ni), None, None, None,
+                                        None), "windows")
+    starts = np.zeros(max(nw.value, 1), np.int64)
+    lens = np.zeros(max(nw.value, 1), np.int32)
+    frames = np.zeros(max(nw.value, 1), np.int32)
+    idx = np.zeros(max(ni.value, 1), np.int32)
+    _check(None, lib().cp_video_windows(*args, ct.byref(nw), ct.byref(ni),
+                                        starts.ctypes.data_as(_abi.I64P),
+                                        lens.ctypes.data_as(_abi.I32P),
+                                        idx.ctypes.data_as(_abi.I32P),
+                                        frames.ctypes.data_as(_abi.I32P)), "windows")
+    return [(int(frames[k]), [int(v) for v in idx[starts[k]:starts[k] + lens[k]]])
+            for k in range(nw.value)]

@@ -1,0 +1,155 @@
+// cp_batch.cpp — many stacks in one persistent launch (cp_composite_batch_device).
+//
+// Replaces the rayon loop of src/main.rs:254-330, which builds one OutlierProcessor per
+// chrono-video window and re-reads every frame for each. Here the windows reference frames
+// already resident on the device; their (stack, tile) work items are flattened through a
+// prefix sum and pulled by persistent CTAs from a device counter. The memset of the counter
+// and the kernel are captured once into a CUDA graph per batch plan and replayed while the
+// batch is unchanged.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "../../include/chrono_gpu.h"
+#include "cp_host_internal.h"
+#include "cp_internal.h"
+
+namespace cp {
+
+
+void release_plans(cp_ctx* ctx) {
+  for (auto& p : ctx->plans) {
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->dev) dev_free(ctx, p->dev);
+  }
+  ctx->plans.clear();
+}
+
+static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_n,
+                            cudaStream_t st) {
+  const int n_stacks = static_cast<int>(plan.host.size());
+  StackDev* d_stacks = static_cast<StackDev*>(plan.dev);
+  int32_t* d_prefix = reinterpret_cast<int32_t*>(d_stacks + n_stacks);
+  uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + n_stacks + 1);
+  const int smem = smem_bytes_for(max_n, kTilePx, channels);
+  int per_sm = 1;
+  switch (channels) {
+    case 1: per_sm = composite_max_ctas_c1(kThreads, smem); break;
+    case 3: per_sm = composite_max_ctas_c3(kThreads, smem); break;
+    default: per_sm = composite_max_ctas_c4(kThreads, smem); break;
+  }
+  const int grid = std::max(1, std::min(plan.total, per_sm * ctx->sm_count));
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "memset");
+  int rc = 0;
+  switch (channels) {
+    case 1: rc = launch_batch_c1(d_stacks, d_prefix, n_stacks, plan.total, d_counter, ctx->d_error, grid, smem, st); break;
+    case 3: rc = launch_batch_c3(d_stacks, d_prefix, n_stacks, plan.total, d_counter, ctx->d_error, grid, smem, st); break;
+    default: rc = launch_batch_c4(d_stacks, d_prefix, n_stacks, plan.total, d_counter, ctx->d_error, grid, smem, st); break;
+  }
+  return cuda_status(ctx, static_cast<cudaError_t>(rc), "batch launch");
+}
+
+}  // namespace cp
+
+using namespace cp;
+
+extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
+                                         const cp_params* params, int32_t n_stacks,
+                                         uint8_t* const* outs, uint8_t* const* out_blends,
+                                         uint64_t* warnings, void* stream) {
+  if (!ctx || !stacks || !params || !outs || n_stacks < 1) return CP_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  std::vector<StackDev> host(static_cast<size_t>(n_stacks));
+  const int channels = stacks[0].channels;
+  int max_n = 0;
+  std::vector<int32_t> prefix(static_cast<size_t>(n_stacks) + 1, 0);
+  std::vector<const uint8_t*> fr;
+  for (int i = 0; i < n_stacks; ++i) {
+    const cp_stack& s = stacks[i];
+    if (s.channels != channels) {
+      ctx_error(ctx, "a batch must have one channel count");
+      return CP_ERR_ARG;
+    }
+    if (s.n < 1 || s.n > CP_MAX_FRAMES || !outs[i]) return CP_ERR_ARG;
+    fr.assign(static_cast<size_t>(s.n), nullptr);
+    for (int f = 0; f < s.n; ++f)
+      fr[static_cast<size_t>(f)] = s.frames ? s.frames[f] : s.base + s.frame_stride * f;
+    StackDev& d = host[static_cast<size_t>(i)];
+    int rc = prepare_stack(ctx, &s, &params[i], fr.data(), &d);
+    if (rc) return rc;
+    d.out = outs[i];
+    d.blend = (out_blends && params[i].mode == CP_MODE_OUTLIER) ? out_blends[i] : nullptr;
+    d.warnings = warnings ? reinterpret_cast<unsigned long long*>(warnings + i) : nullptr;
+    max_n = std::max(max_n, s.n);
+    prefix[static_cast<size_t>(i) + 1] = prefix[static_cast<size_t>(i)] + d.tiles;
+  }
+  if (smem_bytes_for(max_n, kTilePx, channels) > ctx->max_smem) return CP_ERR_ARG;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+
+  // find a plan with the same descriptors
+  BatchPlan* plan = nullptr;
+  for (auto& p : ctx->plans) {
+    if (p->host.size() == host.size() &&
+        std::memcmp(p->host.data(), host.data(), host.size() * sizeof(StackDev)) == 0) {
+      plan = p.get();
+      break;
+    }
+  }
+  if (!plan) {
+    if (ctx->plans.size() >= 8) {  // keep a few plans; drop the oldest
+      cudaStreamSynchronize(st);
+      auto& old = ctx->plans.front();
+      if (old->exec) cudaGraphExecDestroy(old->exec);
+      if (old->graph) cudaGraphDestroy(old->graph);
+      if (old->dev) dev_free(ctx, old->dev);
+      ctx->plans.erase(ctx->plans.begin());
+    }
+    std::unique_ptr<BatchPlan> np(new BatchPlan());
+    np->host = host;
+    np->total = prefix.back();
+    np->dev_bytes = sizeof(StackDev) * host.size() + sizeof(int32_t) * prefix.size() + 64;
+    int rc = dev_alloc(ctx, np->dev_bytes, &np->dev);
+    if (rc) return rc;
+    uint8_t* base = static_cast<uint8_t*>(np->dev);
+    cudaError_t e = cudaMemcpy(base, host.data(), sizeof(StackDev) * host.size(),
+                               cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(base + sizeof(StackDev) * host.size(), prefix.data(),
+                     sizeof(int32_t) * prefix.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      dev_free(ctx, np->dev);
+      return cuda_status(ctx, e, "batch descriptors");
+    }
+    // capture memset + persistent kernel into a graph
+    cudaStream_t cap;
+    cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      rc = batch_launch_raw(ctx, *np, channels, max_n, cap);
+      cudaGraph_t g = nullptr;
+      cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+      if (rc == CP_OK && e2 == cudaSuccess) {
+        np->graph = g;
+        e = cudaGraphInstantiate(&np->exec, g, 0);
+      } else {
+        if (g) cudaGraphDestroy(g);
+        e = e2 != cudaSuccess ? e2 : cudaErrorUnknown;
+      }
+    }
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess || rc != CP_OK) {
+      if (np->graph) cudaGraphDestroy(np->graph);
+      dev_free(ctx, np->dev);
+      return rc ? rc : cuda_status(ctx, e, "batch graph");
+    }
+    ctx->plans.push_back(std::move(np));
+    plan = ctx->plans.back().get();
+  }
+  return cuda_status(ctx, cudaGraphLaunch(plan->exec, st), "graph launch");
+}

@@ -1,0 +1,642 @@
+// cp_host.cpp — C ABI of libchrono_gpu.so: option preparation, contexts, device memory,
+// host staging and the launch plans of the compositing, batch and shake kernels.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/chrono_gpu.h"
+#include "cp_host_internal.h"
+#include "cp_internal.h"
+
+using namespace cp;
+
+// ---------------------------------------------------------------------------------------------
+// Helpers and option semantics (host side)
+// ---------------------------------------------------------------------------------------------
+namespace cp {
+
+void ctx_error(cp_ctx* ctx, const char* fmt, ...) {
+  if (!ctx) return;
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  std::lock_guard<std::mutex> lk(ctx->err_mu);
+  ctx->last_error = buf;
+}
+
+int cuda_status(cp_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return CP_OK;
+  ctx_error(ctx, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return CP_ERR_OOM;
+  return CP_ERR_CUDA;
+}
+
+// Fade::new / Fade::get / fade() (src/options.rs:69-139, src/chrono.rs:496-502).
+int fade_lut(const cp_fade* f, int32_t n, int32_t frame_offset, float* out) {
+  if (n < 0 || (n > 0 && !out)) return CP_ERR_ARG;
+  if (!f || !f->enabled) {
+    for (int i = 0; i < n; ++i) out[i] = 1.0f;
+    return CP_OK;
+  }
+  if (f->n_points < 2 || !f->frames || !f->values) return CP_ERR_ARG;
+  const int32_t offset = f->frames[0];
+  const int32_t last = f->frames[f->n_points - 1];
+  if (last < offset) return CP_ERR_ARG;
+  const size_t len = static_cast<size_t>(last - offset);
+  std::vector<float> values(len + 1, 1.0f);
+  size_t idx = 0;
+  for (size_t i = 0; i < len + 1; ++i) {
+    if (idx + 1 >= static_cast<size_t>(f->n_points)) return CP_ERR_ARG;
+    const int32_t f1 = f->frames[idx], f2 = f->frames[idx + 1];
+    const float v1 = f->values[idx], v2 = f->values[idx + 1];
+    const int32_t frame = static_cast<int32_t>(i) + offset;
+    // v1 + (v2 - v1) * (frame - f1) as f32 / (f2 - f1) as f32, left to right
+    values[i] = v1 + (v2 - v1) * static_cast<float>(frame - f1) / static_cast<float>(f2 - f1);
+    if (frame == f2) idx += 1;
+  }
+  const int32_t vlen = static_cast<int32_t>(values.size());
+  auto get = [&](int32_t frame) -> float {
+    int32_t i = frame - offset;
+    if (i >= 0 && i < vlen) return values[static_cast<size_t>(i)];
+    if (!f->repeat) return i < 0 ? values[0] : values[static_cast<size_t>(vlen - 1)];
+    while (i < 0) i += vlen;
+    return values[static_cast<size_t>(i % vlen)];
+  };
+  for (int32_t i = 0; i < n; ++i) out[i] = f->absolute ? get(frame_offset + i) : get(n - i - 1);
+  return CP_OK;
+}
+
+// quantile() index resolution of src/chrono.rs:567-579 for a sample of `len` values.
+static void quantile_spec(int len, float q, int32_t* k, int32_t* pair, float* frac) {
+  const float pos = static_cast<float>(len + 1) * q;
+  const int p1 = static_cast<int>(pos) - 1;
+  const float fr = pos - std::trunc(pos);
+  if (fr < 0.001f) {
+    *k = p1;
+    *pair = 0;
+    *frac = 0.0f;
+  } else if (fr > 0.999f) {
+    *k = p1 + 1;
+    *pair = 0;
+    *frac = 0.0f;
+  } else {
+    *k = p1;
+    *pair = 1;
+    *frac = fr;
+  }
+}
+
+int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
+                  const uint8_t* const* dev_frames, StackDev* d) {
+  if (!st || !p || !d) return CP_ERR_ARG;
+  const int n = st->n;
+  if (n < 1 || n > CP_MAX_FRAMES) {
+    ctx_error(ctx, "stack of %d frames: supported 1..%d", n, CP_MAX_FRAMES);
+    return CP_ERR_ARG;
+  }
+  if (st->width < 1 || st->height < 1 ||
+      static_cast<int64_t>(st->width) * st->height > (int64_t(1) << 30)) {
+    ctx_error(ctx, "image size %dx%d unsupported", st->width, st->height);
+    return CP_ERR_ARG;
+  }
+  if (st->channels != 1 && st->channels != 3 && st->channels != 4) {
+    ctx_error(ctx, "%d channels unsupported (1, 3 or 4)", st->channels);
+    return CP_ERR_ARG;
+  }
+  if (p->mode < CP_MODE_OUTLIER || p->mode > CP_MODE_LIGHTER) return CP_ERR_ARG;
+  if (p->mode == CP_MODE_OUTLIER) {
+    if (p->outlier < CP_OUTLIER_FIRST || p->outlier > CP_OUTLIER_BACKWARD) return CP_ERR_ARG;
+    if (p->background < CP_BG_FIRST || p->background > CP_BG_MEDIAN) return CP_ERR_ARG;
+  }
+  std::memset(d, 0, sizeof(*d));
+  d->n = n;
+  d->width = st->width;
+  d->height = st->height;
+  d->channels = st->channels;
+  d->has_crop = st->crop != nullptr;
+  d->src_width = d->has_crop ? st->src_width : st->width;
+  if (d->has_crop) {
+    if (st->src_width < st->width || st->src_height < st->height) return CP_ERR_ARG;
+    for (int i = 0; i < n; ++i) {
+      const int cx = st->crop[2 * i], cy = st->crop[2 * i + 1];
+      if (cx < 0 || cy < 0 || cx + st->width > st->src_width || cy + st->height > st->src_height) {
+        ctx_error(ctx, "crop origin (%d,%d) of frame %d outside the source", cx, cy, i);
+        return CP_ERR_ARG;
+      }
+      d->crop[2 * i] = cx;
+      d->crop[2 * i + 1] = cy;
+    }
+  }
+  bool shifted = d->has_crop;
+  for (int i = 0; i < n; ++i) {
+    d->frames[i] = dev_frames[i];
+    if (!dev_frames[i]) return CP_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(dev_frames[i]) & 15) shifted = true;
+  }
+  d->shifted = shifted;
+  d->threads = kThreads;
+  d->tile_px = kTilePx;
+  d->nw = n <= 32 ? 1 : (n <= 64 ? 2 : 4);
+  d->px_begin = 0;
+  d->px_end = st->width * st->height;
+  d->row_begin = 0;
+  if (d->has_crop) {
+    d->tiles_per_row = (st->width + kTilePx - 1) / kTilePx;
+    d->tiles = d->tiles_per_row * st->height;
+  } else {
+    d->tiles_per_row = 0;
+    d->tiles = (d->px_end + kTilePx - 1) / kTilePx;
+  }
+  // options
+  d->mode = p->mode;
+  d->outlier = p->outlier;
+  d->background = p->background;
+  d->thr_abs = p->thr_abs ? 1 : 0;
+  bool unit = true, neg = false;
+  uint32_t wmask = 0;
+  for (int c = 0; c < 4; ++c) {
+    d->w[c] = p->weights[c];
+    if (c < st->channels && p->weights[c] != 0.0f) wmask |= 1u << c;
+    if (c < st->channels && !(p->weights[c] == 0.0f || p->weights[c] == 1.0f)) unit = false;
+    if (c < st->channels && std::signbit(p->weights[c]) && p->weights[c] != 0.0f) neg = true;
+    if (c < st->channels && std::isnan(p->weights[c])) neg = true;
+  }
+  d->wmask = wmask;
+  d->neg_w = neg ? 1u : 0u;
+  d->fast_int = (d->thr_abs && unit) ? 1u : 0u;
+  // Threshold::new, src/options.rs:197-213 (f32 arithmetic)
+  if (d->thr_abs) {
+    d->thr_min = p->thr_min * 255.0f;
+    d->thr_max = p->thr_max * 255.0f;
+    d->thr_scale = 1.0f / ((p->thr_max - p->thr_min) * 255.0f);
+  } else {
+    d->thr_min = p->thr_min;
+    d->thr_max = p->thr_max;
+    d->thr_scale = 1.0f / (p->thr_max - p->thr_min);
+  }
+  d->thr_sq = d->thr_min * d->thr_min;  // src/chrono.rs:220
+  for (int nh = 0; nh <= 4; ++nh) {
+    // smallest integer D' with D' + nh/4 >= thr_sq (exact in double)
+    const double need = static_cast<double>(d->thr_sq) - 0.25 * nh;
+    double t;
+    if (std::isnan(need))
+      t = 2147483647.0;
+    else
+      t = std::ceil(need);
+    if (t < 0) t = 0;
+    if (t > 2147483647.0) t = 2147483647.0;
+    d->thr_int[nh] = static_cast<int32_t>(t);
+  }
+  // (sub)sample for the order statistics
+  int len = n;
+  d->sample_mask[0] = d->sample_mask[1] = d->sample_mask[2] = d->sample_mask[3] = 0;
+  if (p->sample && p->n_sample > 0 && p->n_sample < n) {
+    len = p->n_sample;
+    int prev = -1;
+    for (int i = 0; i < p->n_sample; ++i) {
+      const int s = p->sample[i];
+      if (s <= prev || s >= n) {
+        ctx_error(ctx, "sample indices must be sorted, distinct and < n");
+        return CP_ERR_ARG;
+      }
+      prev = s;
+      d->sample_mask[s >> 5] |= 1u << (s & 31);
+    }
+  } else {
+    for (int i = 0; i < n; ++i) d->sample_mask[i >> 5] |= 1u << (i & 31);
+  }
+  d->n_sub = len;
+  if (p->mode == CP_MODE_OUTLIER && !p->thr_abs && len < 3) {
+    ctx_error(ctx, "relative threshold needs at least 3 samples (got %d)", len);
+    return CP_ERR_ARG;
+  }
+  // median(), src/chrono.rs:582-591
+  if ((len + 1) % 2 == 0) {
+    d->med_k = (len + 1) / 2 - 1;
+    d->med_pair = 0;
+  } else {
+    d->med_k = (len + 1) / 2 - 1;
+    d->med_pair = 1;
+  }
+  if (!p->thr_abs) {
+    quantile_spec(len, 0.25f, &d->q1_k, &d->q1_pair, &d->q1_frac);
+    quantile_spec(len, 0.75f, &d->q3_k, &d->q3_pair, &d->q3_frac);
+  }
+  d->seed = p->rng_seed;
+  if (fade_lut(&p->fade, n, st->frame_offset, d->fade) != CP_OK) {
+    ctx_error(ctx, "invalid fade specification");
+    return CP_ERR_ARG;
+  }
+  return CP_OK;
+}
+
+int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
+  const int smem = smem_bytes_for(d.n, d.tile_px, d.channels);
+  if (smem > ctx->max_smem) {
+    ctx_error(ctx, "tile needs %d bytes of shared memory", smem);
+    return CP_ERR_ARG;
+  }
+  int per_sm = 1, rc = 0;
+  const auto key = std::make_pair(d.channels, smem);
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->occupancy.find(key);
+    if (it != ctx->occupancy.end()) {
+      per_sm = it->second;
+    } else {
+      switch (d.channels) {
+        case 1: per_sm = composite_max_ctas_c1(d.threads, smem); break;
+        case 3: per_sm = composite_max_ctas_c3(d.threads, smem); break;
+        default: per_sm = composite_max_ctas_c4(d.threads, smem); break;
+      }
+      ctx->occupancy[key] = per_sm;
+    }
+  }
+  const int grid = std::max(1, std::min(d.tiles, per_sm * ctx->sm_count));
+  switch (d.channels) {
+    case 1: rc = launch_composite_c1(d, grid, smem, stream, ctx->d_error); break;
+    case 3: rc = launch_composite_c3(d, grid, smem, stream, ctx->d_error); break;
+    default: rc = launch_composite_c4(d, grid, smem, stream, ctx->d_error); break;
+  }
+  return cuda_status(ctx, static_cast<cudaError_t>(rc), "composite launch");
+}
+
+int check_device_error(cp_ctx* ctx) {
+  uint32_t err = 0;
+  cudaError_t e = cudaMemcpy(&err, ctx->d_error, sizeof err, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "error flag read");
+  if (err) {
+    cudaMemset(ctx->d_error, 0, sizeof err);
+    ctx_error(ctx, "a device-side wait timed out (error flags 0x%x)", err);
+    return CP_ERR_TIMEOUT;
+  }
+  return CP_OK;
+}
+
+int budget_reserve(cp_ctx* ctx, uint64_t bytes) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (ctx->budget && ctx->used + bytes > ctx->budget) {
+    ctx_error(ctx, "HBM budget exceeded: %llu + %llu > %llu", (unsigned long long)ctx->used,
+              (unsigned long long)bytes, (unsigned long long)ctx->budget);
+    return CP_ERR_BUDGET;
+  }
+  ctx->used += bytes;
+  return CP_OK;
+}
+void budget_release(cp_ctx* ctx, uint64_t bytes) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->used = bytes > ctx->used ? 0 : ctx->used - bytes;
+}
+
+int dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr) {
+  if (!ptr) return CP_ERR_ARG;
+  *ptr = nullptr;
+  if (bytes == 0) return CP_OK;
+  int rc = budget_reserve(ctx, bytes);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    budget_release(ctx, bytes);
+    *ptr = nullptr;
+    return cuda_status(ctx, e, "cudaMalloc");
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->allocs[*ptr] = bytes;
+  return CP_OK;
+}
+
+int dev_free(cp_ctx* ctx, void* ptr) {
+  if (!ptr) return CP_OK;
+  uint64_t bytes = 0;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->allocs.find(ptr);
+    if (it == ctx->allocs.end()) return CP_ERR_ARG;
+    bytes = it->second;
+    ctx->allocs.erase(it);
+  }
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaFree(ptr);
+  budget_release(ctx, bytes);
+  return cuda_status(ctx, e, "cudaFree");
+}
+
+// Grows a context-owned device buffer to at least `bytes`.
+int ensure_buffer(cp_ctx* ctx, DevBuffer& b, uint64_t bytes) {
+  if (b.bytes >= bytes) return CP_OK;
+  if (b.ptr) {
+    int rc = dev_free(ctx, b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    if (rc) return rc;
+  }
+  void* p = nullptr;
+  int rc = dev_alloc(ctx, bytes, &p);
+  if (rc) return rc;
+  b.ptr = p;
+  b.bytes = bytes;
+  return CP_OK;
+}
+
+int ensure_pinned(cp_ctx* ctx, PinnedBuffer& b, uint64_t bytes) {
+  if (b.bytes >= bytes) return CP_OK;
+  if (b.ptr) cudaFreeHost(b.ptr);
+  b.ptr = nullptr;
+  b.bytes = 0;
+  cudaError_t e = cudaHostAlloc(&b.ptr, bytes, cudaHostAllocPortable);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "cudaHostAlloc");
+  b.bytes = bytes;
+  return CP_OK;
+}
+
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+}  // namespace cp
+
+// ---------------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+const char* cp_version(void) { return "chrono-gpu 0.1.0 (sm_103a)"; }
+
+const char* cp_status_str(int status) {
+  switch (status) {
+    case CP_OK: return "ok";
+    case CP_ERR_ARG: return "invalid argument";
+    case CP_ERR_OOM: return "out of memory";
+    case CP_ERR_TIMEOUT: return "timed out";
+    case CP_ERR_CUDA: return "CUDA error";
+    case CP_ERR_BUDGET: return "HBM budget exceeded";
+    case CP_ERR_RANGE: return "coordinate out of range";
+    case CP_ERR_STATE: return "invalid state";
+    case CP_ERR_NODEV: return "no sm_103 device";
+    default: return "unknown status";
+  }
+}
+
+void cp_params_default(cp_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->mode = CP_MODE_OUTLIER;
+  p->thr_abs = 1;
+  p->thr_min = 0.05f;
+  p->thr_max = 0.2f;
+  p->outlier = CP_OUTLIER_EXTREME;
+  p->background = CP_BG_RANDOM;
+  for (float& w : p->weights) w = 1.0f;
+  p->fade.enabled = 0;
+  p->rng_seed = 0x5EEDull;
+}
+
+int cp_fade_lut(const cp_fade* fade, int32_t n, int32_t frame_offset, float* out) {
+  return fade_lut(fade, n, frame_offset, out);
+}
+
+int cp_video_windows(int32_t image_count, int32_t in_has_start, int32_t in_start,
+                     int32_t in_has_end, int32_t in_end, int32_t in_step, int32_t out_has_start,
+                     int32_t out_start, int32_t out_has_end, int32_t out_end, int32_t out_step,
+                     int32_t* n_windows, int64_t* n_indices, int64_t* win_start, int32_t* win_len,
+                     int32_t* win_indices, int32_t* win_frame) {
+  // create_video window arithmetic, src/main.rs:230-286
+  if (!n_windows || !n_indices || in_step <= 0 || out_step <= 0) return CP_ERR_ARG;
+  int32_t v_lower;
+  if (out_has_start)
+    v_lower = out_start;
+  else if (in_has_start && in_has_end)
+    v_lower = -(in_end - in_start) + 1;
+  else
+    v_lower = 0;
+  const int32_t v_upper = out_has_end ? out_end : image_count;
+  int32_t count = (v_upper - v_lower) / out_step;
+  if (count < 0) count = 0;
+  int64_t total = 0;
+  for (int32_t k = 0; k < count; ++k) {
+    const int32_t frame = k * out_step + v_lower;
+    int32_t start = 0;
+    if (in_has_start) {
+      int32_t s = frame + in_start;
+      while (s < 0) s += in_step;
+      start = std::max(s % in_step, frame + in_start);
+    }
+    int32_t end = image_count;
+    if (in_has_end) end = std::min(image_count + (frame + in_end) % in_step - in_step, frame + in_end);
+    int32_t len = 0;
+    for (int32_t f = start; f < end; f += in_step) {
+      if (win_indices) win_indices[total + len] = f;
+      ++len;
+    }
+    if (win_start) win_start[k] = total;
+    if (win_len) win_len[k] = len;
+    if (win_frame) win_frame[k] = frame - v_lower;
+    total += len;
+  }
+  *n_windows = count;
+  *n_indices = total;
+  return CP_OK;
+}
+
+int cp_crop_create(const int32_t* offsets, int32_t n, int32_t width, int32_t height,
+                   int32_t* has_crop, int32_t* crops) {
+  // Crop::create, src/shake.rs:136-176
+  if (!offsets || n < 0 || !has_crop) return CP_ERR_ARG;
+  int32_t xmin = 0, ymin = 0, xmax = 0, ymax = 0;
+  for (int i = 0; i < n; ++i) {
+    xmin = std::min(xmin, offsets[2 * i]);
+    ymin = std::min(ymin, offsets[2 * i + 1]);
+    xmax = std::max(xmax, offsets[2 * i]);
+    ymax = std::max(ymax, offsets[2 * i + 1]);
+  }
+  if (xmin == 0 && ymin == 0 && xmax == 0 && ymax == 0) {
+    *has_crop = 0;
+    return CP_OK;
+  }
+  if (!crops) return CP_ERR_ARG;
+  *has_crop = 1;
+  const int32_t w = width + xmin - xmax, h = height + ymin - ymax;
+  for (int i = 0; i < n; ++i) {
+    crops[4 * i] = offsets[2 * i] - xmin;
+    crops[4 * i + 1] = offsets[2 * i + 1] - ymin;
+    crops[4 * i + 2] = w;
+    crops[4 * i + 3] = h;
+  }
+  return CP_OK;
+}
+
+int cp_sample_indices(int32_t n, int32_t count, uint64_t seed, int32_t* out, int32_t* n_out) {
+  if (n < 0 || count < 0 || !out || !n_out) return CP_ERR_ARG;
+  if (count >= n) {  // src/chrono.rs:153-154
+    for (int i = 0; i < n; ++i) out[i] = i;
+    *n_out = n;
+    return CP_OK;
+  }
+  // partial Fisher-Yates with a splitmix64 stream, then sorted (src/chrono.rs:156-158)
+  std::vector<int32_t> idx(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) idx[static_cast<size_t>(i)] = i;
+  uint64_t x = seed;
+  for (int i = 0; i < count; ++i) {
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const int j = i + static_cast<int>(((z >> 32) * static_cast<uint64_t>(n - i)) >> 32);
+    std::swap(idx[static_cast<size_t>(i)], idx[static_cast<size_t>(j)]);
+  }
+  std::sort(idx.begin(), idx.begin() + count);
+  for (int i = 0; i < count; ++i) out[i] = idx[static_cast<size_t>(i)];
+  *n_out = count;
+  return CP_OK;
+}
+
+int cp_ctx_create(int32_t device, uint64_t hbm_budget, cp_ctx** out) {
+  if (!out) return CP_ERR_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return CP_ERR_NODEV;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return CP_ERR_NODEV;
+  if (prop.major != 10 || prop.minor != 3) return CP_ERR_NODEV;  // built for sm_103a only
+  if (cudaSetDevice(device) != cudaSuccess) return CP_ERR_NODEV;
+  std::unique_ptr<cp_ctx> ctx(new cp_ctx());
+  ctx->device = device;
+  ctx->budget = hbm_budget;
+  ctx->sm_count = prop.multiProcessorCount;
+  ctx->max_smem = static_cast<int>(prop.sharedMemPerBlockOptin);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return CP_ERR_CUDA;
+  void* p = nullptr;
+  if (dev_alloc(ctx.get(), 256, &p) != CP_OK) return CP_ERR_OOM;
+  ctx->d_error = static_cast<uint32_t*>(p);
+  ctx->d_warn = reinterpret_cast<unsigned long long*>(static_cast<uint8_t*>(p) + 64);
+  if (cudaMemset(p, 0, 256) != cudaSuccess) return CP_ERR_CUDA;
+  *out = ctx.release();
+  return CP_OK;
+}
+
+void cp_ctx_destroy(cp_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamSynchronize(ctx->copy_stream);
+  cudaStreamSynchronize(ctx->d2h_stream);
+  release_plans(ctx);
+  std::vector<void*> ptrs;
+  for (auto& kv : ctx->allocs) ptrs.push_back(kv.first);
+  for (void* q : ptrs) cudaFree(q);
+  for (auto& pb : {&ctx->pin_in, &ctx->pin_out, &ctx->pin_blend})
+    if (pb->ptr) cudaFreeHost(pb->ptr);
+  for (auto& ev : ctx->band_events) cudaEventDestroy(ev);
+  cudaStreamDestroy(ctx->stream);
+  cudaStreamDestroy(ctx->copy_stream);
+  cudaStreamDestroy(ctx->d2h_stream);
+  delete ctx;
+}
+
+int cp_ctx_last_error(cp_ctx* ctx, char* buf, size_t len) {
+  if (!ctx || !buf || len == 0) return CP_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->err_mu);
+  std::snprintf(buf, len, "%s", ctx->last_error.c_str());
+  return CP_OK;
+}
+
+void* cp_ctx_stream(cp_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
+
+int cp_ctx_synchronize(cp_ctx* ctx) {
+  if (!ctx) return CP_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int rc = cuda_status(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
+  if (rc) return rc;
+  return check_device_error(ctx);
+}
+
+int cp_dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr) {
+  if (!ctx) return CP_ERR_ARG;
+  return dev_alloc(ctx, bytes, ptr);
+}
+int cp_dev_free(cp_ctx* ctx, void* ptr) {
+  if (!ctx) return CP_ERR_ARG;
+  return dev_free(ctx, ptr);
+}
+int cp_host_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr) {
+  if (!ctx || !ptr) return CP_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  return cuda_status(ctx, cudaHostAlloc(ptr, bytes, cudaHostAllocPortable), "cudaHostAlloc");
+}
+int cp_host_free(cp_ctx* ctx, void* ptr) {
+  if (!ctx) return CP_ERR_ARG;
+  return cuda_status(ctx, cudaFreeHost(ptr), "cudaFreeHost");
+}
+int cp_memcpy_h2d(cp_ctx* ctx, void* dst, const void* src, uint64_t bytes, void* stream) {
+  if (!ctx) return CP_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  int rc = cuda_status(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "h2d");
+  if (rc || stream) return rc;
+  return cuda_status(ctx, cudaStreamSynchronize(st), "h2d sync");
+}
+int cp_memcpy_d2h(cp_ctx* ctx, void* dst, const void* src, uint64_t bytes, void* stream) {
+  if (!ctx) return CP_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  int rc = cuda_status(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st), "d2h");
+  if (rc || stream) return rc;
+  return cuda_status(ctx, cudaStreamSynchronize(st), "d2h sync");
+}
+
+int cp_composite_device(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                        uint8_t* out, uint8_t* out_blend, const cp_debug* dbg,
+                        uint64_t* warnings, void* stream) {
+  if (!ctx || !stack || !params || !out) return CP_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  std::vector<const uint8_t*> fr(static_cast<size_t>(std::max(stack->n, 0)));
+  for (int i = 0; i < stack->n && i < CP_MAX_FRAMES; ++i)
+    fr[static_cast<size_t>(i)] = stack->frames ? stack->frames[i] : stack->base + stack->frame_stride * i;
+  if (stack->n < 1 || stack->n > CP_MAX_FRAMES) return CP_ERR_ARG;
+  std::unique_ptr<StackDev> d(new StackDev());
+  int rc = prepare_stack(ctx, stack, params, fr.data(), d.get());
+  if (rc) return rc;
+  d->out = out;
+  d->blend = params->mode == CP_MODE_OUTLIER ? out_blend : nullptr;
+  d->warnings = reinterpret_cast<unsigned long long*>(warnings);
+  if (dbg && params->mode == CP_MODE_OUTLIER) {
+    d->dbg_median = dbg->median;
+    d->dbg_q1 = dbg->q1;
+    d->dbg_q3 = dbg->q3;
+    d->dbg_bits = dbg->outlier_bits;
+    d->dbg_chosen = dbg->chosen;
+    d->dbg_bg = dbg->background;
+    d->dbg_nout = dbg->n_outliers;
+  }
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  return launch_single(ctx, *d, st);
+}
+
+}  // extern "C"

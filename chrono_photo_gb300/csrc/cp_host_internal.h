@@ -1,0 +1,81 @@
+// cp_host_internal.h — the context object and host helpers shared by the C-ABI sources.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/chrono_gpu.h"
+#include "cp_internal.h"
+
+namespace cp {
+
+struct DevBuffer {
+  void* ptr = nullptr;
+  uint64_t bytes = 0;
+};
+struct PinnedBuffer {
+  void* ptr = nullptr;
+  uint64_t bytes = 0;
+};
+
+// One captured batch launch (cp_batch.cpp).
+struct BatchPlan {
+  std::vector<StackDev> host;  // descriptors the plan was built from
+  void* dev = nullptr;         // [StackDev x n][int32 prefix x (n+1)][uint32 counter]
+  uint64_t dev_bytes = 0;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int32_t total = 0;
+};
+
+}  // namespace cp
+
+struct cp_ctx {
+  int device = 0;
+  int sm_count = 0;
+  int max_smem = 0;
+  cudaStream_t stream = nullptr;       // kernels
+  cudaStream_t copy_stream = nullptr;  // host -> device staging
+  cudaStream_t d2h_stream = nullptr;   // device -> host results
+  uint64_t budget = 0, used = 0;
+  std::mutex mu;      // allocations, budget, caches
+  std::mutex err_mu;  // last_error
+  std::mutex call_mu; // serialises the host-staged entry points (shared staging buffers)
+  std::string last_error;
+  std::map<void*, uint64_t> allocs;
+  std::map<std::pair<int, int>, int> occupancy;  // (channels, smem) -> CTAs per SM
+  uint32_t* d_error = nullptr;               // device error flags of bounded waits
+  unsigned long long* d_warn = nullptr;      // device warning counter (host-staged calls)
+  // host-staged composite: device copies of the frames and outputs, pinned staging
+  cp::DevBuffer frames_dev, out_dev, blend_dev, dbg_dev;
+  cp::PinnedBuffer pin_in, pin_out, pin_blend;
+  std::vector<cudaEvent_t> band_events;
+  // batch plans (graph-captured persistent launches)
+  std::vector<std::unique_ptr<cp::BatchPlan>> plans;
+};
+
+namespace cp {
+
+void ctx_error(cp_ctx* ctx, const char* fmt, ...);
+int cuda_status(cp_ctx* ctx, cudaError_t e, const char* what);
+int fade_lut(const cp_fade* f, int32_t n, int32_t frame_offset, float* out);
+int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
+                  const uint8_t* const* dev_frames, StackDev* d);
+int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream);
+int check_device_error(cp_ctx* ctx);
+int budget_reserve(cp_ctx* ctx, uint64_t bytes);
+void budget_release(cp_ctx* ctx, uint64_t bytes);
+int dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr);
+int dev_free(cp_ctx* ctx, void* ptr);
+int ensure_buffer(cp_ctx* ctx, DevBuffer& b, uint64_t bytes);
+int ensure_pinned(cp_ctx* ctx, PinnedBuffer& b, uint64_t bytes);
+bool is_pinned(const void* p);
+void release_plans(cp_ctx* ctx);
+
+}  // namespace cp

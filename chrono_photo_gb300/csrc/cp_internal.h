@@ -1,0 +1,87 @@
+// cp_internal.h — types shared by the host layer (cp_host.cpp) and the CUDA kernels.
+#pragma once
+#include <cstdint>
+
+#include "../../include/chrono_gpu.h"
+
+namespace cp {
+
+constexpr int kPixPerThread = 4;   // a thread owns 4 pixels = `channels` words per frame row
+constexpr int kThreads = 64;       // CTA size of the compositing kernels
+constexpr int kTilePx = kPixPerThread * kThreads;
+
+// Device-side descriptor of one stack and its options, prepared on the host from cp_stack
+// and cp_params. A single-stack launch passes it by value (kernel parameter space, so the
+// per-frame tables need no device allocation); a batch keeps an array in device memory.
+struct StackDev {
+  // geometry
+  int32_t n, width, height, channels;
+  int32_t src_width;      // row pitch (pixels) of the source frames
+  int32_t tiles;          // work items of this stack
+  int32_t tiles_per_row;  // > 0: tiles are row segments (cropped stacks); 0: flat pixel ranges
+  int32_t tile_px;        // pixels per tile
+  int32_t px_begin;       // flat tiles: first output pixel covered (row bands)
+  int32_t px_end;         //             one past the last
+  int32_t row_begin;      // row tiles: first output row covered
+  int32_t nw;             // 32-frame words per bit plane: 1, 2 or 4
+  int32_t threads;        // CTA size the stack was planned for
+  int32_t has_crop;
+  int32_t shifted;        // some frame row may start off a 16-byte boundary
+  // outputs
+  uint8_t* out;
+  uint8_t* blend;
+  unsigned long long* warnings;
+  float* dbg_median;
+  float* dbg_q1;
+  float* dbg_q3;
+  uint32_t* dbg_bits;
+  int32_t* dbg_chosen;
+  int32_t* dbg_bg;
+  int32_t* dbg_nout;
+  // options
+  int32_t mode, outlier, background, thr_abs;
+  float w[4];
+  uint32_t wmask;      // bit c: weights[c] != 0
+  uint32_t fast_int;   // abs threshold and every weight 0 or 1: exact integer distances
+  uint32_t neg_w;      // some weight negative
+  float thr_min, thr_max, thr_scale, thr_sq;
+  int32_t thr_int[5];  // smallest integer D' with D' + nh/4 >= thr_sq, per nh = 0..4
+  // order statistics of the (sub)sample (quantile/median, src/chrono.rs:567-591)
+  int32_t n_sub;
+  int32_t med_k, med_pair;
+  int32_t q1_k, q1_pair;
+  float q1_frac;
+  int32_t q3_k, q3_pair;
+  float q3_frac;
+  uint32_t sample_mask[4];  // frames in the (sub)sample, bit i of word i/32
+  uint64_t seed;
+  // per-frame tables
+  const uint8_t* frames[CP_MAX_FRAMES];
+  int32_t crop[2 * CP_MAX_FRAMES];
+  float fade[CP_MAX_FRAMES];  // fade(i, n, frame_offset)
+};
+
+inline int row_pitch_host(int tile_px, int channels) { return tile_px * channels + 32; }
+inline int smem_bytes_for(int n, int tile_px, int channels) {
+  return 256 + n * row_pitch_host(tile_px, channels);
+}
+
+// Per-channel-count kernel entry points (cp_kernels_c*.cu). Return cudaError_t values.
+#define CP_DECLARE_CH(CH)                                                                 \
+  int composite_max_ctas_c##CH(int threads, int smem);                                    \
+  int launch_composite_c##CH(const StackDev& s, int grid, int smem, void* stream,         \
+                             uint32_t* error);                                            \
+  int launch_batch_c##CH(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks, \
+                         int32_t total, uint32_t* counter, uint32_t* error, int grid,     \
+                         int smem, void* stream);
+CP_DECLARE_CH(1)
+CP_DECLARE_CH(3)
+CP_DECLARE_CH(4)
+#undef CP_DECLARE_CH
+
+// Shake search (cp_shake.cu): diffs[(f-1) * S^2 + oy*S + ox] for frames 1..n-1.
+int launch_shake(const uint8_t* const* frames_dev, int32_t n, int32_t width, int32_t height,
+                 int32_t channels, const int32_t* anchors_dev, int32_t n_anchors, int32_t r,
+                 int32_t s, int32_t* diffs_dev, void* stream);
+
+}  // namespace cp

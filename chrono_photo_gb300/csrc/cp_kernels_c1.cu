@@ -1,0 +1,32 @@
+// Instantiates the compositing kernels for 1-channel images and their launchers.
+#include "cp_tile.cuh"
+
+namespace cp {
+
+int composite_max_ctas_c1(int threads, int smem) {
+  const void* fn = reinterpret_cast<const void*>(&k_composite<1>);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess)
+    return 1;
+  return blocks < 1 ? 1 : blocks;
+}
+
+int launch_composite_c1(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
+  cudaFuncSetAttribute(reinterpret_cast<const void*>(&k_composite<1>),
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  k_composite<1><<<grid, s.threads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int launch_batch_c1(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks,
+                     int32_t total, uint32_t* counter, uint32_t* error, int grid, int smem,
+                     void* stream) {
+  cudaFuncSetAttribute(reinterpret_cast<const void*>(&k_composite_batch<1>),
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  k_composite_batch<1><<<grid, 64, smem, static_cast<cudaStream_t>(stream)>>>(
+      stacks, prefix, n_stacks, total, counter, error);
+  return static_cast<int>(cudaGetLastError());
+}
+
+}  // namespace cp

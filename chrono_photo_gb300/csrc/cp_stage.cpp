@@ -1,0 +1,180 @@
+// cp_stage.cpp — host-memory compositing (cp_composite): the replacement of the
+// reference's time-slice pipeline (src/slicer.rs, src/streams.rs, the per-slice loop of
+// src/chrono.rs:96-193). Whole frames are copied to the device in row bands on a copy
+// stream; the kernel of band b runs while band b+1 is in flight, and each band's result is
+// copied back on a third stream as soon as its kernel is done.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/chrono_gpu.h"
+#include "cp_host_internal.h"
+#include "cp_internal.h"
+
+using namespace cp;
+
+namespace {
+
+constexpr uint64_t kFrameAlign = 256;  // device frame pitch: keeps every frame 16-byte aligned
+
+uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+int ensure_events(cp_ctx* ctx, size_t count) {
+  while (ctx->band_events.size() < count) {
+    cudaEvent_t e;
+    cudaError_t rc = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (rc != cudaSuccess) return cuda_status(ctx, rc, "cudaEventCreate");
+    ctx->band_events.push_back(e);
+  }
+  return CP_OK;
+}
+
+}  // namespace
+
+extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                            uint8_t* out, uint8_t* out_blend, const cp_debug* dbg,
+                            uint64_t* n_warnings) {
+  if (!ctx || !stack || !params || !out) return CP_ERR_ARG;
+  if (stack->n < 1 || stack->n > CP_MAX_FRAMES || (!stack->frames && !stack->base))
+    return CP_ERR_ARG;
+  std::lock_guard<std::mutex> call(ctx->call_mu);
+  cudaSetDevice(ctx->device);
+  const int n = stack->n, C = stack->channels;
+  const bool crop = stack->crop != nullptr;
+  const int sw = crop ? stack->src_width : stack->width;
+  const int sh = crop ? stack->src_height : stack->height;
+  if (sw < 1 || sh < 1 || C < 1 || C > 4) return CP_ERR_ARG;
+  const uint64_t frame_bytes = static_cast<uint64_t>(sw) * sh * C;
+  const uint64_t pitch = round_up(frame_bytes + 16, kFrameAlign);
+  const uint64_t P = static_cast<uint64_t>(stack->width) * stack->height;
+  const uint64_t out_bytes = P * C;
+  int rc = ensure_buffer(ctx, ctx->frames_dev, pitch * n);
+  if (!rc) rc = ensure_buffer(ctx, ctx->out_dev, round_up(out_bytes, 256));
+  const bool want_blend = out_blend && params->mode == CP_MODE_OUTLIER;
+  if (!rc && want_blend) rc = ensure_buffer(ctx, ctx->blend_dev, round_up(out_bytes, 256));
+  if (rc) return rc;
+
+  // device frame table
+  uint8_t* fdev = static_cast<uint8_t*>(ctx->frames_dev.ptr);
+  std::vector<const uint8_t*> dev_frames(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) dev_frames[static_cast<size_t>(i)] = fdev + pitch * i;
+  StackDev d;
+  rc = prepare_stack(ctx, stack, params, dev_frames.data(), &d);
+  if (rc) return rc;
+  d.out = static_cast<uint8_t*>(ctx->out_dev.ptr);
+  d.blend = want_blend ? static_cast<uint8_t*>(ctx->blend_dev.ptr) : nullptr;
+  d.warnings = ctx->d_warn;
+
+  // optional diagnostics: device arrays, copied back at the end
+  const int words = (n + 31) / 32;
+  struct DbgPart {
+    void* host;
+    uint64_t bytes;
+    uint64_t off;
+  };
+  std::vector<DbgPart> parts;
+  if (dbg && params->mode == CP_MODE_OUTLIER) {
+    uint64_t off = 0;
+    auto add = [&](void* h, uint64_t bytes) {
+      if (!h) return;
+      parts.push_back({h, bytes, off});
+      off += round_up(bytes, 256);
+    };
+    add(dbg->median, P * C * 4);
+    add(dbg->q1, P * C * 4);
+    add(dbg->q3, P * C * 4);
+    add(dbg->outlier_bits, P * words * 4);
+    add(dbg->chosen, P * 4);
+    add(dbg->background, P * 4);
+    add(dbg->n_outliers, P * 4);
+    if (off) {
+      rc = ensure_buffer(ctx, ctx->dbg_dev, off);
+      if (rc) return rc;
+      uint8_t* base = static_cast<uint8_t*>(ctx->dbg_dev.ptr);
+      size_t k = 0;
+      auto ptr = [&](void* h) -> void* { return h ? base + parts[k++].off : nullptr; };
+      d.dbg_median = static_cast<float*>(ptr(dbg->median));
+      d.dbg_q1 = static_cast<float*>(ptr(dbg->q1));
+      d.dbg_q3 = static_cast<float*>(ptr(dbg->q3));
+      d.dbg_bits = static_cast<uint32_t*>(ptr(dbg->outlier_bits));
+      d.dbg_chosen = static_cast<int32_t*>(ptr(dbg->chosen));
+      d.dbg_bg = static_cast<int32_t*>(ptr(dbg->background));
+      d.dbg_nout = static_cast<int32_t*>(ptr(dbg->n_outliers));
+    }
+  }
+
+  rc = cuda_status(ctx, cudaMemsetAsync(ctx->d_warn, 0, sizeof(unsigned long long), ctx->stream),
+                   "memset");
+  if (rc) return rc;
+
+  // bands: flat pixel ranges in whole tiles; cropped stacks move whole frames at once
+  int bands = 1;
+  if (!crop && P >= static_cast<uint64_t>(kTilePx) * ctx->sm_count * 4) bands = 4;
+  rc = ensure_events(ctx, static_cast<size_t>(2 * bands));
+  if (rc) return rc;
+  const uint64_t tiles_total = (P + kTilePx - 1) / kTilePx;
+  auto host_frame = [&](int i) -> const uint8_t* {
+    return stack->frames ? stack->frames[i] : stack->base + stack->frame_stride * i;
+  };
+  for (int b = 0; b < bands; ++b) {
+    const uint64_t t0 = tiles_total * b / bands, t1 = tiles_total * (b + 1) / bands;
+    const uint64_t px0 = t0 * kTilePx, px1 = std::min<uint64_t>(t1 * kTilePx, P);
+    if (px1 <= px0) continue;
+    // frames (or their band) host -> device
+    for (int i = 0; i < n; ++i) {
+      const uint8_t* src = host_frame(i);
+      if (crop) {
+        rc = cuda_status(ctx, cudaMemcpyAsync(fdev + pitch * i, src, frame_bytes,
+                                              cudaMemcpyHostToDevice, ctx->copy_stream), "h2d");
+      } else {
+        rc = cuda_status(ctx, cudaMemcpyAsync(fdev + pitch * i + px0 * C, src + px0 * C,
+                                              (px1 - px0) * C, cudaMemcpyHostToDevice,
+                                              ctx->copy_stream), "h2d");
+      }
+      if (rc) return rc;
+    }
+    cudaEvent_t copied = ctx->band_events[static_cast<size_t>(2 * b)];
+    cudaEvent_t done = ctx->band_events[static_cast<size_t>(2 * b + 1)];
+    cudaEventRecord(copied, ctx->copy_stream);
+    cudaStreamWaitEvent(ctx->stream, copied, 0);
+    StackDev db = d;
+    if (!crop) {
+      db.px_begin = static_cast<int32_t>(px0);
+      db.px_end = static_cast<int32_t>(px1);
+      db.tiles = static_cast<int32_t>(t1 - t0);
+    }
+    rc = launch_single(ctx, db, ctx->stream);
+    if (rc) return rc;
+    cudaEventRecord(done, ctx->stream);
+    cudaStreamWaitEvent(ctx->d2h_stream, done, 0);
+    const uint64_t o0 = crop ? 0 : px0 * C, ob = crop ? out_bytes : (px1 - px0) * C;
+    rc = cuda_status(ctx, cudaMemcpyAsync(out + o0, d.out + o0, ob, cudaMemcpyDeviceToHost,
+                                          ctx->d2h_stream), "d2h");
+    if (!rc && want_blend)
+      rc = cuda_status(ctx, cudaMemcpyAsync(out_blend + o0, d.blend + o0, ob,
+                                            cudaMemcpyDeviceToHost, ctx->d2h_stream), "d2h");
+    if (rc) return rc;
+  }
+  uint64_t warn = 0;
+  cudaEvent_t all = ctx->band_events[0];
+  cudaEventRecord(all, ctx->stream);
+  cudaStreamWaitEvent(ctx->d2h_stream, all, 0);
+  rc = cuda_status(ctx, cudaMemcpyAsync(&warn, ctx->d_warn, sizeof warn, cudaMemcpyDeviceToHost,
+                                        ctx->d2h_stream), "d2h");
+  if (rc) return rc;
+  for (const auto& part : parts) {
+    rc = cuda_status(ctx, cudaMemcpyAsync(part.host, static_cast<uint8_t*>(ctx->dbg_dev.ptr) + part.off,
+                                          part.bytes, cudaMemcpyDeviceToHost, ctx->d2h_stream),
+                     "d2h");
+    if (rc) return rc;
+  }
+  rc = cuda_status(ctx, cudaStreamSynchronize(ctx->d2h_stream), "synchronize");
+  if (rc) return rc;
+  rc = check_device_error(ctx);
+  if (rc) return rc;
+  if (n_warnings) *n_warnings = warn;
+  return CP_OK;
+}

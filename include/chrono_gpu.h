@@ -1,0 +1,256 @@
+/*
+ * chrono_gpu.h — C ABI of the GB300 frame-stack compositing library (libchrono_gpu.so).
+ *
+ * Replaces the stack reduction of chrono-photo 0.6.5 (a Rust CLI/library):
+ *   - OutlierProcessor::new/process ............ src/chrono.rs:46-206 (per-pixel calc_pixel :208-494)
+ *   - SimpleProcessor::new/process (darker/lighter) src/simple.rs:18-168
+ *   - ShakeAnalyzer::analyze / Crop::create .... src/shake.rs:136-176, :190-313
+ *   - chrono-video window enumeration .......... src/main.rs:214-331
+ * The reference has no FFI; these entry points are what a Rust crate would bind with
+ * `extern "C"` in place of the calls at src/main.rs:465-483 (create_frame),
+ * :504-511 (create_frame_simple) and :61-74 (shake analysis).
+ *
+ * Conventions
+ *   - Every function returns an int status: CP_OK (0) or a negative CP_ERR_* code.
+ *     The reference panics on layout mismatches (src/chrono.rs:126, src/simple.rs:65,
+ *     src/shake.rs:336); here those cases return CP_ERR_ARG / CP_ERR_RANGE instead.
+ *   - Buffers are caller-owned. Images are interleaved 8-bit, row-major, `channels`
+ *     bytes per pixel (1..4), the flat layout of image::FlatSamples used by the reference.
+ *   - Stacks are frame-major: frame i of a stack is `frames[i]` (per-frame pointers) or
+ *     `base + i * frame_stride`.
+ *   - `*_device` entry points take device pointers and a CUDA stream (cudaStream_t passed
+ *     as void*, NULL = the context's own stream) and are asynchronous unless noted.
+ *     Entry points without the suffix take host memory and are synchronous.
+ *   - No CPU fallback: if no usable sm_103 device is present, cp_ctx_create fails.
+ */
+#ifndef CHRONO_GPU_H
+#define CHRONO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define CP_OK 0
+#define CP_ERR_ARG (-1)     /* invalid argument or unsupported layout                      */
+#define CP_ERR_OOM (-2)     /* device or pinned allocation failed                          */
+#define CP_ERR_TIMEOUT (-3) /* a bounded device-side wait gave up (persistent queue)       */
+#define CP_ERR_CUDA (-4)    /* CUDA runtime error; see cp_ctx_last_error                   */
+#define CP_ERR_BUDGET (-5)  /* request exceeds the HBM budget of the context/server        */
+#define CP_ERR_RANGE (-6)   /* shake window outside the image (reference: panic, shake.rs:336) */
+#define CP_ERR_STATE (-7)   /* object in the wrong state (stopped server, unknown job)     */
+#define CP_ERR_NODEV (-8)   /* no CUDA device with compute capability 10.3                 */
+
+/* ---- option enums (src/options.rs) --------------------------------------------------- */
+/* SelectionMode, src/options.rs:8-31 */
+#define CP_MODE_OUTLIER 0
+#define CP_MODE_DARKER 1
+#define CP_MODE_LIGHTER 2
+/* OutlierSelectionMode, src/options.rs:284-315 */
+#define CP_OUTLIER_FIRST 0
+#define CP_OUTLIER_LAST 1
+#define CP_OUTLIER_EXTREME 2
+#define CP_OUTLIER_AVERAGE 3
+#define CP_OUTLIER_FORWARD 4
+#define CP_OUTLIER_BACKWARD 5
+/* BackgroundMode, src/options.rs:319-344 */
+#define CP_BG_FIRST 0
+#define CP_BG_RANDOM 1
+#define CP_BG_AVERAGE 2
+#define CP_BG_MEDIAN 3
+
+/* Largest stack (frames per composite) the kernels accept. */
+#define CP_MAX_FRAMES 128
+
+/* Fade, src/options.rs:60-139. Points are (frame, value) pairs ordered by frame, as
+ * parsed from `(clamp|repeat)/(abs|rel)/f,v/f,v/...`. enabled = 0 is Fade::none(). */
+typedef struct cp_fade {
+  int32_t enabled;
+  int32_t repeat;   /* 1: FadeMode::Repeat, 0: FadeMode::Clamp */
+  int32_t absolute; /* 1: abs (frame index + window offset), 0: rel (counted from the end) */
+  int32_t n_points; /* >= 2 when enabled */
+  const int32_t* frames;
+  const float* values;
+} cp_fade;
+
+/* Parsed CLI options for one composite (src/cli.rs:22-136; defaults src/cli.rs:192-216).
+ * Threshold values are the raw CLI numbers; the abs scaling by 255 of
+ * Threshold::new (src/options.rs:197-213) happens inside. */
+typedef struct cp_params {
+  int32_t mode;       /* CP_MODE_*                                        */
+  int32_t thr_abs;    /* 1: abs/min/max, 0: rel/min/max                   */
+  float thr_min;      /* --threshold min                                  */
+  float thr_max;      /* --threshold max (the parser copies min if absent) */
+  int32_t outlier;    /* CP_OUTLIER_*                                     */
+  int32_t background; /* CP_BG_*                                          */
+  float weights[4];   /* --weights, per channel                           */
+  cp_fade fade;       /* --fade                                           */
+  /* --sample: sorted, distinct sample positions (0..n-1) used for the median/quartiles
+   * (src/chrono.rs:151-163, :227-235). NULL / 0 = all frames. The reference draws them
+   * with an unseeded RNG; cp_sample_indices draws them from a seed. */
+  const int32_t* sample;
+  int32_t n_sample;
+  /* Seed of the counter-based generator that replaces the reference's unseeded
+   * ThreadRng for --background random (src/chrono.rs:355-360, :532-555). */
+  uint64_t rng_seed;
+} cp_params;
+
+/* One frame stack. With `crop` set, output pixel (x, y) of frame i is read from source
+ * pixel (x + crop[2i], y + crop[2i+1]) of a src_width x src_height frame: the per-frame
+ * crop origins of Crop::create (src/shake.rs:136-176) applied as address offsets. */
+typedef struct cp_stack {
+  int32_t n;        /* frames (samples) in the stack, 1..CP_MAX_FRAMES               */
+  int32_t width;    /* output width  (cropped width when crop != NULL)                */
+  int32_t height;   /* output height                                                  */
+  int32_t channels; /* bytes per pixel, 1..4 (layout.width_stride)                    */
+  const uint8_t* const* frames; /* per-frame base pointers, or NULL to use base/stride */
+  const uint8_t* base;
+  int64_t frame_stride;         /* bytes between frames when frames == NULL           */
+  const int32_t* crop;          /* NULL or 2*n crop origins (x, y)                    */
+  int32_t src_width;            /* source frame size when crop != NULL                */
+  int32_t src_height;
+  /* indices[0] of a chrono-video window: the `frame_offset` that an absolute fade is
+   * evaluated at (src/chrono.rs:103, :496-502; src/simple.rs:54-57). 0 for a still. */
+  int32_t frame_offset;
+} cp_stack;
+
+/* Optional per-pixel diagnostics of the outlier kernel, device (or host for the host
+ * entry point) arrays; any member may be NULL. P = width * height. */
+typedef struct cp_debug {
+  float* median;          /* [P][channels] median (0 for weight-0 channels), chrono.rs:238-255 */
+  float* q1;              /* [P][channels] lower quartile (rel threshold only)                 */
+  float* q3;              /* [P][channels] upper quartile (rel threshold only)                 */
+  uint32_t* outlier_bits; /* [P][words] bit i set iff sample i is an outlier, words = (n+31)/32 */
+  int32_t* chosen;        /* [P] sample index blended in (-1: none; forward/backward with >1
+                             outliers: -2; average with >1 outliers: 0, the index the reference
+                             evaluates the fade at, chrono.rs:467)                              */
+  int32_t* background;    /* [P] sample index copied as background (first/random), else -1    */
+  int32_t* n_outliers;    /* [P] number of outliers                                           */
+} cp_debug;
+
+/* ---- library / options helpers (host only) ------------------------------------------- */
+const char* cp_version(void);
+const char* cp_status_str(int status);
+/* Defaults of src/cli.rs:192-216: outlier, abs/0.05/0.2, background random, outlier
+ * extreme, weights 1 1 1 1, fade none. */
+void cp_params_default(cp_params* p);
+/* Fade factor of every sample of an n-frame stack: out[i] = fade(i, n, frame_offset) with
+ * the Fade::new table and Fade::get lookup (src/options.rs:69-139, src/chrono.rs:496-502). */
+int cp_fade_lut(const cp_fade* fade, int32_t n, int32_t frame_offset, float* out);
+/* Chrono-video windows (src/main.rs:230-286). Ranges are FrameRange start/end/step with
+ * has_* = 0 for the `.` placeholder (src/flist.rs:46-79). Writes, for each output frame k,
+ * win_start[k] = offset into win_indices and win_len[k] (0 = skipped frame). Pass NULL
+ * buffers to query *n_windows and *n_indices first. */
+int cp_video_windows(int32_t image_count, int32_t in_has_start, int32_t in_start,
+                     int32_t in_has_end, int32_t in_end, int32_t in_step,
+                     int32_t out_has_start, int32_t out_start, int32_t out_has_end,
+                     int32_t out_end, int32_t out_step, int32_t* n_windows,
+                     int64_t* n_indices, int64_t* win_start, int32_t* win_len,
+                     int32_t* win_indices, int32_t* win_frame);
+/* Crop::create (src/shake.rs:136-176): crops[4i..4i+3] = (x, y, w, h) per frame.
+ * *has_crop = 0 (and crops untouched) when every offset is (0, 0) — the reference's None. */
+int cp_crop_create(const int32_t* offsets, int32_t n, int32_t width, int32_t height,
+                   int32_t* has_crop, int32_t* crops);
+/* Seeded replacement for rand::seq::sample_indices + sort (src/chrono.rs:153-158):
+ * writes min(count, n) sorted distinct positions. */
+int cp_sample_indices(int32_t n, int32_t count, uint64_t seed, int32_t* out, int32_t* n_out);
+
+/* ---- context ------------------------------------------------------------------------- */
+typedef struct cp_ctx cp_ctx;
+/* hbm_budget: bytes of device memory the context may hold (0 = no limit). */
+int cp_ctx_create(int32_t device, uint64_t hbm_budget, cp_ctx** out);
+void cp_ctx_destroy(cp_ctx* ctx);
+/* Copies the last error message of this context into buf (always NUL-terminated). */
+int cp_ctx_last_error(cp_ctx* ctx, char* buf, size_t len);
+/* Stream the *_device entry points use when passed NULL. */
+void* cp_ctx_stream(cp_ctx* ctx);
+int cp_ctx_synchronize(cp_ctx* ctx);
+/* Device memory owned by the context (counted against its HBM budget). */
+int cp_dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr);
+int cp_dev_free(cp_ctx* ctx, void* ptr);
+/* Pinned (page-locked) host memory: frames staged from it are copied by DMA without an
+ * intermediate host copy. */
+int cp_host_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr);
+int cp_host_free(cp_ctx* ctx, void* ptr);
+/* stream NULL: synchronous on the context's stream. */
+int cp_memcpy_h2d(cp_ctx* ctx, void* dst_dev, const void* src_host, uint64_t bytes, void* stream);
+int cp_memcpy_d2h(cp_ctx* ctx, void* dst_host, const void* src_dev, uint64_t bytes, void* stream);
+
+/* ---- compositing --------------------------------------------------------------------- */
+/* One stack per launch (the plain kernel). Device pointers throughout: frames (16-byte
+ * aligned, each readable up to the next multiple of 16 bytes past its last pixel), out
+ * (P*channels bytes), out_blend (P*channels, nullable; outlier mode only: the blend mask,
+ * 255 in channels >= 3, src/chrono.rs:183-191), dbg members. warnings (device uint64,
+ * nullable) is incremented by the number of all-outlier pixels (src/chrono.rs:180-203).
+ * Replaces OutlierProcessor::process (mode outlier) and SimpleProcessor::process
+ * (darker/lighter) for one output frame. */
+int cp_composite_device(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                        uint8_t* out, uint8_t* out_blend, const cp_debug* dbg,
+                        uint64_t* warnings, void* stream);
+
+/* Host-memory form of cp_composite_device: frames in host memory are staged through
+ * pinned buffers and copied to the device in row bands that overlap the kernel; results
+ * are copied back. Synchronous. n_warnings (host, nullable) receives the warning count.
+ * dbg members, when given, are host arrays. */
+int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params* params, uint8_t* out,
+                 uint8_t* out_blend, const cp_debug* dbg, uint64_t* n_warnings);
+
+/* Many stacks of uneven size in ONE persistent launch that pulls (stack, tile) work items
+ * from a device queue (chrono-video windows, mixed jobs). Device pointers; params[i]
+ * applies to stacks[i]; outs/blends/warnings are per stack (blends/warnings nullable).
+ * The launch is captured into a CUDA graph that is replayed while the batch shape is
+ * unchanged. Replaces the rayon loop over create_frame calls, src/main.rs:254-330. */
+int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks, const cp_params* params,
+                              int32_t n_stacks, uint8_t* const* outs,
+                              uint8_t* const* out_blends, uint64_t* warnings, void* stream);
+
+/* ---- camera shake -------------------------------------------------------------------- */
+/* ShakeAnalyzer::analyze (src/shake.rs:190-313): anchor windows of radius anchor_radius
+ * from frame 0, exhaustive wrapping-i32 sum of squared differences over the
+ * (2*search_radius+1)^2 offsets for frames 1..n-1, first minimum. Device frames; offsets
+ * (host, 2n int32, frame 0 = (0, 0)) and, nullable, diffs (host, (n-1)*(2s+1)^2 int32) are
+ * written on return (synchronous). CP_ERR_RANGE where the reference would panic. */
+int cp_shake_analyze_device(cp_ctx* ctx, const uint8_t* const* frames, int32_t n,
+                            int32_t width, int32_t height, int32_t channels,
+                            const int32_t* anchors, int32_t n_anchors, int32_t anchor_radius,
+                            int32_t search_radius, int32_t* offsets, int32_t* diffs);
+
+/* ---- serving ------------------------------------------------------------------------- */
+/* A compositing job: a host-memory stack plus options, output buffers in host memory.
+ * Frames named by (frame_keys) are kept resident on the device between jobs, so jobs
+ * over overlapping windows of the same frames share uploads; key 0 = not shareable. */
+typedef struct cp_job {
+  cp_stack stack;              /* host frames (frames[] or base/stride)                */
+  const uint64_t* frame_keys;  /* nullable: n keys naming the frames for residency    */
+  cp_params params;
+  uint8_t* out;                /* host, width*height*channels                          */
+  uint8_t* out_blend;          /* host, nullable                                       */
+} cp_job;
+
+typedef struct cp_job_result {
+  int32_t status;              /* CP_OK or the job's error                             */
+  uint64_t warnings;
+  double submit_s;             /* host clock (s) at submit, admission, completion      */
+  double admit_s;
+  double done_s;
+} cp_job_result;
+
+typedef struct cp_server cp_server;
+/* max_inflight: jobs whose work may be on the device at once. The server admits jobs
+ * against the context's HBM budget (hbm_budget, 0 = the context's) as memory frees up and
+ * merges the tiles of all admitted jobs into the running persistent launches. */
+int cp_server_create(cp_ctx* ctx, uint64_t hbm_budget, int32_t max_inflight, cp_server** out);
+/* Non-blocking; the job's buffers must stay valid until it completes. */
+int cp_server_submit(cp_server* srv, const cp_job* job, uint64_t* job_id);
+/* Waits up to timeout_ms (-1 = forever) for job_id. CP_ERR_TIMEOUT if not done yet. */
+int cp_server_wait(cp_server* srv, uint64_t job_id, int32_t timeout_ms, cp_job_result* res);
+/* Stops accepting jobs, drains the queue and joins the worker. */
+int cp_server_destroy(cp_server* srv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHRONO_GPU_H */

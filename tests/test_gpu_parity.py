@@ -1,0 +1,198 @@
+"""CUDA kernels against the oracle through the C ABI (needs a GB300).
+
+Bit-exact: median, quartiles, outlier flags, chosen index, background index, outlier count
+and warnings. Composite and blend mask: within 1 LSB per band (the benchmark spec's tolerance);
+the kernels reproduce the reference's f32 operation order, so the error is expected to be 0
+and the max/mean error is reported."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from chrono_photo_gb300 import _abi, example_data
+from oracle import oracle
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+OUTLIERS = ["first", "last", "extreme", "average", "forward", "backward"]
+BACKGROUNDS = ["first", "random", "average", "median"]
+
+
+def compare(ctx, frames, offset=0, crop=None, out_size=None, **kw):
+    p = cases.params(**kw)
+    ref = oracle.composite(frames, p, frame_offset=offset, crop=crop, out_size=out_size,
+                           debug=kw.get("mode", "outlier") == "outlier", threads=8)
+    if crop is not None:
+        got = ctx.composite(frames, p, frame_offset=offset, crop=(crop, out_size),
+                            debug=kw.get("mode", "outlier") == "outlier")
+    else:
+        got = ctx.composite(frames, p, frame_offset=offset,
+                            debug=kw.get("mode", "outlier") == "outlier")
+    err = cases.assert_close_u8(got[0], ref[0], what="composite")
+    if kw.get("mode", "outlier") == "outlier":
+        cases.assert_close_u8(got[1], ref[1], what="blend mask")
+        assert got[2] == ref[2], "warnings"
+        g, r = got[3], ref[3]
+        for k in ("median", "outlier_bits", "chosen", "background", "n_outliers"):
+            assert np.array_equal(g[k], r[k]), k
+        if not p.thr_abs:
+            assert np.array_equal(g["q1"], r["q1"]) and np.array_equal(g["q3"], r["q3"])
+    return err
+
+
+@pytest.mark.parametrize("case", cases.kat()["pixels"], ids=lambda c: c["name"])
+def test_pixel_kat_gpu(ctx, case):
+    st = cases.pixel_stack(case["samples"])
+    p = cases.params(mode="outlier", threshold=case["threshold"], outlier=case["outlier"],
+                     background=case["background"], weights=case["weights"], fade=case.get("fade"))
+    out, blend, warn = ctx.composite(st, p)
+    assert out.reshape(-1).tolist() == case["expect_pixel"]
+    assert blend.reshape(-1)[0] == case["expect_mask"]
+
+
+@pytest.mark.parametrize("case", cases.kat()["simple"], ids=lambda c: c["name"])
+def test_simple_kat_gpu(ctx, case):
+    st = cases.pixel_stack(case["samples"])
+    p = cases.params(mode="darker" if case["darker"] else "lighter", weights=case["weights"],
+                     fade=case.get("fade"))
+    assert ctx.composite(st, p, blend=False)[0].reshape(-1).tolist() == case["expect_pixel"]
+
+
+@pytest.fixture(scope="module")
+def small():
+    """16 frames of 640x480 with a moving r=20 disk (seed 1), at half size for speed."""
+    return example_data.small_stack(seed=1, scale=2)
+
+
+@pytest.mark.parametrize("outlier", OUTLIERS)
+def test_small_stack_outlier_modes(ctx, small, outlier):
+    compare(ctx, small, mode="outlier", threshold="abs/0.05/0.2", outlier=outlier,
+            background="first")
+
+
+@pytest.mark.parametrize("background", BACKGROUNDS)
+def test_small_stack_backgrounds(ctx, small, background):
+    compare(ctx, small, mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+            background=background, seed=99)
+
+
+@pytest.mark.parametrize("outlier", ["average", "forward", "backward", "extreme"])
+def test_rel_threshold(ctx, small, outlier):
+    compare(ctx, small, mode="outlier", threshold="rel/3/6", outlier=outlier, background="first")
+
+
+@pytest.mark.parametrize("mode", ["darker", "lighter"])
+def test_simple(ctx, small, mode):
+    compare(ctx, small, mode=mode)
+    compare(ctx, small, mode=mode, weights=[0.3, 0.59, 0.11, 1], fade="clamp/abs/0,0/8,1")
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 7, 8, 16, 31, 32, 33, 63, 64, 65, 100, 127, 128])
+def test_frame_counts(ctx, n):
+    rng = np.random.default_rng(n)
+    frames = cases.random_stack(rng, n, 13, 37, 3, n_spots=6)
+    compare(ctx, frames, mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+            background="first")
+    compare(ctx, frames, mode="outlier", threshold="abs/0.03/0.1", outlier="forward",
+            background="average")
+    if n >= 3:
+        compare(ctx, frames, mode="outlier", threshold="rel/2/4", outlier="average",
+                background="median")
+
+
+@pytest.mark.parametrize("c", [1, 3, 4])
+@pytest.mark.parametrize("shape", [(1, 1), (3, 5), (17, 29), (64, 64), (33, 300)])
+def test_shapes_channels(ctx, c, shape):
+    rng = np.random.default_rng(c * 100 + shape[0])
+    frames = cases.random_stack(rng, 12, shape[0], shape[1], c)
+    compare(ctx, frames, mode="outlier", threshold="abs/0.05/0.2", outlier="last",
+            background="first", weights=[1, 1, 1, 0])
+    compare(ctx, frames, mode="lighter")
+
+
+@pytest.mark.parametrize("weights", [[1, 1, 0, 1], [0.5, 1, 2, 1], [1, -1, 1, 1], [0, 0, 1, 1]])
+def test_weights(ctx, weights):
+    rng = np.random.default_rng(5)
+    frames = cases.random_stack(rng, 20, 31, 41, 3)
+    compare(ctx, frames, mode="outlier", threshold="abs/0.05/0.2", outlier="forward",
+            background="median", weights=weights)
+    compare(ctx, frames, mode="outlier", threshold="rel/1.5/3", outlier="extreme",
+            background="average", weights=weights)
+
+
+@pytest.mark.parametrize("fade_s,offset", [("clamp/abs/0,0/10,1", 0), ("repeat/abs/2,1/5,0.25", 7),
+                                           ("clamp/rel/0,1/4,0", 0)])
+def test_fades(ctx, fade_s, offset):
+    rng = np.random.default_rng(9)
+    frames = cases.random_stack(rng, 14, 20, 30, 3)
+    for outlier in ("backward", "average", "extreme"):
+        compare(ctx, frames, offset=offset, mode="outlier", threshold="abs/0.04/0.3",
+                outlier=outlier, background="first", fade=fade_s)
+
+
+def test_sample_subset(ctx):
+    rng = np.random.default_rng(12)
+    frames = cases.random_stack(rng, 40, 20, 30, 3)
+    compare(ctx, frames, mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+            background="first", sample=[0, 3, 4, 8, 11, 20, 33, 39])
+    compare(ctx, frames, mode="outlier", threshold="rel/3/6", outlier="last",
+            background="median", sample=list(range(1, 40, 3)))
+
+
+@pytest.mark.parametrize("thr", ["abs/0/0.1", "abs/1/1", "abs/0.02", "rel/0/1", "rel/0.5"])
+def test_threshold_edges(ctx, thr):
+    rng = np.random.default_rng(21)
+    frames = cases.random_stack(rng, 9, 16, 16, 3)
+    compare(ctx, frames, mode="outlier", threshold=thr, outlier="extreme", background="first")
+    compare(ctx, frames, mode="outlier", threshold=thr, outlier="forward", background="random")
+
+
+def test_crop_offsets(ctx):
+    """Shake-corrected stacks: per-frame crop origins applied as address offsets."""
+    rng = np.random.default_rng(4)
+    frames = cases.random_stack(rng, 10, 40, 300, 3)
+    offs = np.array([[0, 0], [3, -2], [-1, 4], [5, 1], [-7, -3], [2, 2], [0, 6], [1, -1],
+                     [4, 0], [-2, 5]])
+    crops = oracle.crop_create(offs, 300, 40)
+    origins = crops[:, :2]
+    size = (int(crops[0, 2]), int(crops[0, 3]))
+    compare(ctx, frames, crop=origins, out_size=size, mode="outlier", threshold="abs/0.05/0.2",
+            outlier="extreme", background="first")
+    compare(ctx, frames, crop=origins, out_size=size, mode="darker")
+
+
+def test_device_entry_point_matches_host(ctx, small):
+    """cp_composite_device on device-resident frames equals the host-staged cp_composite."""
+    n, h, w, c = small.shape
+    p = cases.params(mode="outlier", threshold="abs/0.05/0.2", outlier="average",
+                     background="average")
+    ref = ctx.composite(small, p)
+    fb = ctx.upload(small)
+    out = ctx.alloc(h * w * c)
+    bl = ctx.alloc(h * w * c)
+    warn = ctx.alloc(8)
+    ctx.upload(np.zeros(1, np.uint64), warn)
+    try:
+        st = _abi.Stack(n=n, width=w, height=h, channels=c, base=fb, frame_stride=h * w * c)
+        rc = _abi.lib().cp_composite_device(ctx.handle, ct.byref(st), ct.byref(p), out, bl,
+                                            None, warn, None)
+        ctx.check(rc)
+        ctx.synchronize()
+        assert np.array_equal(ctx.download(out, (h, w, c)), ref[0])
+        assert np.array_equal(ctx.download(bl, (h, w, c)), ref[1])
+        assert int(ctx.download(warn, (1,), np.uint64)[0]) == ref[2]
+    finally:
+        for q in (fb, out, bl, warn):
+            ctx.free(q)
+
+
+def test_invalid_stacks(ctx):
+    f = np.zeros((129, 2, 2, 3), np.uint8)
+    with pytest.raises(_abi.ChronoError) as e:
+        ctx.composite(f, cases.params())
+    assert e.value.status == _abi.CP_ERR_ARG
+    with pytest.raises(_abi.ChronoError):
+        ctx.composite(np.zeros((2, 2, 2, 3), np.uint8), cases.params(threshold="rel/1/2"))
+    with pytest.raises(_abi.ChronoError):
+        ctx.composite(np.zeros((4, 2, 2, 2), np.uint8), cases.params())
