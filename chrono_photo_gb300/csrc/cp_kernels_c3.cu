@@ -29,4 +29,20 @@ int launch_batch_c3(const StackDev* stacks, const int32_t* prefix, int32_t n_sta
   return static_cast<int>(cudaGetLastError());
 }
 
+int simple_stream_max_ctas_c3(bool fast) {
+  const void* fn = fast ? reinterpret_cast<const void*>(&k_simple_stream<3, true>)
+                        : reinterpret_cast<const void*>(&k_simple_stream<3, false>);
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 256, 0) != cudaSuccess) return 1;
+  return blocks < 1 ? 1 : blocks;
+}
+
+int launch_simple_stream_c3(const StackDev& s, bool fast, int grid, void* stream) {
+  if (fast)
+    k_simple_stream<3, true><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(s);
+  else
+    k_simple_stream<3, false><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(s);
+  return static_cast<int>(cudaGetLastError());
+}
+
 }  // namespace cp

@@ -134,14 +134,18 @@ DEVI TileGeo tile_geo(const StackDev& S, int t) {
   return g;
 }
 
-__host__ __device__ __forceinline__ int row_pitch(int tile_px, int C) { return tile_px * C + 32; }
+// Shared-memory row pitch of a tile: 4 pixels per thread, plus room for the byte shift of
+// rows copied from below an unaligned source.
+template <int C>
+constexpr int kPitch = kTilePx * C + 32;
 
 // Warp 0 stages the n frame rows of a tile into `buf` (row f at f * pitch). A source that is
 // not 16-byte aligned (cropped stacks, unaligned frames) is copied from the aligned address
 // below it and the offset is recorded in shifts[f]. Must be called by all 32 lanes of warp 0.
 template <int C>
-DEVI void issue_tile(const StackDev& S, const TileGeo& g, uint8_t* buf, int pitch,
-                     uint8_t* shifts, uint64_t* bar) {
+DEVI void issue_tile(const StackDev& S, const TileGeo& g, uint8_t* buf, uint8_t* shifts,
+                     uint64_t* bar) {
+  constexpr int pitch = kPitch<C>;
   const int lane = threadIdx.x & 31;
   const int row_bytes = g.npx * C;
   uint32_t total = 0;
@@ -179,19 +183,27 @@ DEVI void issue_tile(const StackDev& S, const TileGeo& g, uint8_t* buf, int pitc
   }
 }
 
-// Word `word` (0..C-1) of this thread's 4-pixel column in frame row f.
-struct RowReader {
-  const uint8_t* buf;
+
+// ---- shared-memory rows ------------------------------------------------------------------------
+// Word w (0..C-1) of this thread's 4-pixel column in frame row f. SHIFTED rows start
+// shifts[f] bytes into their shared-memory row (sources below a 16-byte boundary).
+template <int C, bool SHIFTED>
+struct Rows {
+  const uint8_t* col;  // shared-memory data + 4 * C * thread
   const uint8_t* shifts;
-  int pitch;
-  int col;  // byte offset of this thread's column: 4 * C * thread
-  bool shifted;  // rows may start off a 16-byte boundary: per-frame byte shift
   DEVI uint32_t word(int f, int w) const {
-    const uint8_t* row = buf + (size_t)f * pitch;
-    if (!shifted) return *reinterpret_cast<const uint32_t*>(row + col + 4 * w);
-    const int off = shifts[f] + col + 4 * w;
-    const uint32_t* r = reinterpret_cast<const uint32_t*>(row + (off & ~3));
-    return __funnelshift_r(r[0], r[1], (off & 3) * 8);
+    const uint8_t* row = col + f * kPitch<C>;
+    if constexpr (!SHIFTED) {
+      return *reinterpret_cast<const uint32_t*>(row + 4 * w);
+    } else {
+      const int off = shifts[f] + 4 * w;
+      const uint32_t* r = reinterpret_cast<const uint32_t*>(row + (off & ~3));
+      return __funnelshift_r(r[0], r[1], (off & 3) * 8);
+    }
+  }
+  DEVI void frame(int f, uint32_t (&wv)[C]) const {
+#pragma unroll
+    for (int i = 0; i < C; ++i) wv[i] = word(f, i);
   }
 };
 
@@ -200,8 +212,6 @@ template <int C>
 DEVI uint32_t pixel_word(const uint32_t (&w)[C], int p) {
   if constexpr (C == 1) {
     return (w[0] >> (8 * p)) & 0xFFu;
-  } else if constexpr (C == 2) {
-    return ((p < 2 ? w[0] : w[1]) >> (16 * (p & 1))) & 0xFFFFu;
   } else if constexpr (C == 3) {
     if (p == 0) return w[0] & 0x00FFFFFFu;
     if (p == 1) return __funnelshift_r(w[0], w[1], 24) & 0x00FFFFFFu;
@@ -211,13 +221,11 @@ DEVI uint32_t pixel_word(const uint32_t (&w)[C], int p) {
     return w[p];
   }
 }
-// Pixel p (runtime 0..3) of frame f, loading only the words it spans.
-template <int C>
-DEVI uint32_t load_pixel(const RowReader& rd, int f, int p) {
+// Same with a runtime pixel index, loading only the words the pixel spans.
+template <int C, bool SH>
+DEVI uint32_t load_pixel(const Rows<C, SH>& rd, int f, int p) {
   if constexpr (C == 1) {
     return (rd.word(f, 0) >> (8 * p)) & 0xFFu;
-  } else if constexpr (C == 2) {
-    return (rd.word(f, p >> 1) >> (16 * (p & 1))) & 0xFFFFu;
   } else if constexpr (C == 3) {
     if (p == 0) return rd.word(f, 0) & 0x00FFFFFFu;
     if (p == 1) return __funnelshift_r(rd.word(f, 0), rd.word(f, 1), 24) & 0x00FFFFFFu;
@@ -228,37 +236,42 @@ DEVI uint32_t load_pixel(const RowReader& rd, int f, int p) {
   }
 }
 
-// ---- bit planes -----------------------------------------------------------------------------
+// Element p of a 4-array held in registers, selected without local memory.
+template <typename T>
+DEVI T pick4(const T (&a)[4], int p) {
+  T v = a[0];
+  v = p == 1 ? a[1] : v;
+  v = p == 2 ? a[2] : v;
+  v = p == 3 ? a[3] : v;
+  return v;
+}
+
+// ---- bit planes ------------------------------------------------------------------------------
 // 8x8 bit transpose of each byte column of 8 words: afterwards a[r] byte k bit i = bit r of
 // byte k of input word i.
 DEVI void transpose8(uint32_t (&a)[8]) {
+  // swap the off-diagonal blocks of each 8x8 bit matrix at scales 4, 2, 1: the bits of b
+  // under M move up by s into a, the bits of a above M move down into b
+  auto swap = [](uint32_t& x, uint32_t& y, int sh, uint32_t m) {
+    const uint32_t nx = (x & ~(m << sh)) | ((y << sh) & (m << sh));
+    const uint32_t ny = (y & ~m) | ((x >> sh) & m);
+    x = nx;
+    y = ny;
+  };
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const uint32_t t = ((a[i] >> 4) ^ a[i + 4]) & 0x0F0F0F0Fu;
-    a[i + 4] ^= t;
-    a[i] ^= t << 4;
-  }
+  for (int i = 0; i < 4; ++i) swap(a[i], a[i + 4], 4, 0x0F0F0F0Fu);
 #pragma unroll
   for (int i = 0; i < 8; i += 4) {
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const uint32_t t = ((a[i + j] >> 2) ^ a[i + j + 2]) & 0x33333333u;
-      a[i + j + 2] ^= t;
-      a[i + j] ^= t << 2;
-    }
+    swap(a[i], a[i + 2], 2, 0x33333333u);
+    swap(a[i + 1], a[i + 3], 2, 0x33333333u);
   }
 #pragma unroll
-  for (int i = 0; i < 8; i += 2) {
-    const uint32_t t = ((a[i] >> 1) ^ a[i + 1]) & 0x55555555u;
-    a[i + 1] ^= t;
-    a[i] ^= t << 1;
-  }
+  for (int i = 0; i < 8; i += 2) swap(a[i], a[i + 1], 1, 0x55555555u);
 }
 
-// Planes of byte positions KP0..KP0+BP-1 of word `w` over all frames: P[k][r][blk] bit i =
-// bit r of the byte of frame 32*blk + i.
-// One 32-frame block of planes: q[k][r] bit i = bit r of byte k of frame 32*blk + i.
-DEVI void planes_block(uint32_t (&q)[4][8], const RowReader& rd, int w, int blk, int n) {
+// One 32-frame block of planes of word w: q[k][r] bit i = bit r of byte k of frame 32*blk+i.
+template <int C, bool SH>
+DEVI void planes_block(uint32_t (&q)[4][8], const Rows<C, SH>& rd, int w, int blk, int n) {
   uint32_t a[4][8];
 #pragma unroll
   for (int g = 0; g < 4; ++g) {
@@ -289,168 +302,93 @@ DEVI void planes_block(uint32_t (&q)[4][8], const RowReader& rd, int w, int blk,
   }
 }
 
-// Planes of byte positions KP0..KP0+BP-1 of word `w` over all frames: P[k][r][blk] bit i =
-// bit r of the byte of frame 32*blk + i. Up to 64 frames the block loop is unrolled; above,
-// a rolled loop shifts each block in from the top.
-template <int C, int NW, int BP, int KP0>
-DEVI void build_planes(uint32_t (&P)[BP][8][NW], const RowReader& rd, int w, int n) {
-  if constexpr (NW <= 2) {
+// Planes of the BP byte positions kp0.. of word w over all frames: P[k][r][blk] bit i = bit
+// r of the byte of frame 32*blk + i. kp0 is 0 when BP == 4, 0 or 2 when BP == 2.
+template <int C, int NW, int BP, bool SH>
+DEVI void build_planes(uint32_t (&P)[BP][8][NW], const Rows<C, SH>& rd, int w, int kp0, int n) {
 #pragma unroll
-    for (int blk = 0; blk < NW; ++blk) {
-      uint32_t q[4][8];
-      planes_block(q, rd, w, blk, n);
+  for (int blk = 0; blk < NW; ++blk) {
+    uint32_t q[4][8];
+    planes_block<C, SH>(q, rd, w, blk, n);
 #pragma unroll
-      for (int k = 0; k < BP; ++k)
+    for (int k = 0; k < BP; ++k)
 #pragma unroll
-        for (int r = 0; r < 8; ++r) P[k][r][blk] = q[KP0 + k][r];
-    }
-  } else {
-#pragma unroll 1
-    for (int blk = 0; blk < NW; ++blk) {
-      uint32_t q[4][8];
-      planes_block(q, rd, w, blk, n);
+      for (int r = 0; r < 8; ++r) P[k][r][blk] = (BP == 4 || kp0 == 0) ? q[k][r] : q[k + BP][r];
+  }
+}
+
+// k-th smallest of the frames in S for BP byte positions at once (independent chains the
+// scheduler interleaves): radix select over the 8 bit planes. On return c holds the frames
+// equal to the result and kk the rank of the k-th among them.
+template <int NW, int BP>
+DEVI void radix_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], const int (&k)[BP],
+                      uint32_t (&res)[BP], uint32_t (&c)[BP][NW], int (&kk)[BP]) {
 #pragma unroll
-      for (int k = 0; k < BP; ++k)
+  for (int j = 0; j < BP; ++j) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+    for (int w = 0; w < NW; ++w) c[j][w] = S[w];
+    kk[j] = k[j];
+    res[j] = 0u;
+  }
 #pragma unroll
-          for (int i = 0; i + 1 < NW; ++i) P[k][r][i] = P[k][r][i + 1];
-          P[k][r][NW - 1] = q[KP0 + k][r];
-        }
+  for (int b = 7; b >= 0; --b) {
+#pragma unroll
+    for (int j = 0; j < BP; ++j) {
+      uint32_t z[NW];
+      int cz = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        z[w] = c[j][w] & ~P[j][b][w];
+        cz += __popc(z[w]);
+      }
+      const bool one = kk[j] >= cz;
+      kk[j] -= one ? cz : 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) c[j][w] = one ? (c[j][w] ^ z[w]) : z[w];  // c & P or c & ~P
+      res[j] = (res[j] << 1) | static_cast<uint32_t>(one);
     }
   }
 }
 
-// k-th smallest (lo) and, when `pair`, (k+1)-th smallest (hi) of the frames in `S` given
-// their bit planes. Radix select over the 8 bits; hi is lo when the run of lo continues,
-// else the minimum of the values above lo.
-template <int NW>
-DEVI void select_pair(const uint32_t (&P)[8][NW], const uint32_t (&S)[NW], int k, bool pair,
-                      uint32_t& lo, uint32_t& hi) {
-  uint32_t c[NW];
+// Order statistics d[k] (lo) and, when `pair`, d[k+1] (hi). d[k+1] equals d[k] while the run
+// of equal values continues past rank k; otherwise a second radix select finds it.
+template <int NW, int BP>
+DEVI void select_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], int k,
+                       bool pair, uint32_t (&lo)[BP], uint32_t (&hi)[BP]) {
+  uint32_t c[BP][NW];
+  int kk[BP], kv[BP];
 #pragma unroll
-  for (int w = 0; w < NW; ++w) c[w] = S[w];
-  int kk = k;
-  uint32_t res = 0;
+  for (int j = 0; j < BP; ++j) kv[j] = k;
+  radix_multi<NW, BP>(P, S, kv, lo, c, kk);
+  bool any = false;
+  bool need[BP];
 #pragma unroll
-  for (int b = 7; b >= 0; --b) {
-    uint32_t z[NW];
-    int cz = 0;
+  for (int j = 0; j < BP; ++j) {
+    hi[j] = lo[j];
+    int ceq = 0;
 #pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      z[w] = c[w] & ~P[b][w];
-      cz += __popc(z[w]);
-    }
-    const bool one = kk >= cz;
-    kk = one ? kk - cz : kk;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) c[w] = one ? (c[w] & P[b][w]) : z[w];
-    res |= static_cast<uint32_t>(one) << b;
+    for (int w = 0; w < NW; ++w) ceq += __popc(c[j][w]);
+    need[j] = pair && kk[j] + 1 >= ceq;
+    any |= need[j];
   }
-  lo = res;
-  hi = res;
-  if (!pair) return;
-  int ceq = 0;
+  if (!__any_sync(0xffffffffu, any)) return;
+  uint32_t r2[BP];
 #pragma unroll
-  for (int w = 0; w < NW; ++w) ceq += __popc(c[w]);
-  const bool need = kk + 1 >= ceq;
-  if (!__any_sync(0xffffffffu, need)) return;
-  uint32_t gt[NW], eq[NW];
+  for (int j = 0; j < BP; ++j) kv[j] = k + 1;
+  radix_multi<NW, BP>(P, S, kv, r2, c, kk);
 #pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    gt[w] = 0u;
-    eq[w] = S[w];
-  }
-#pragma unroll
-  for (int b = 7; b >= 0; --b) {
-    const uint32_t rb = 0u - ((res >> b) & 1u);
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      gt[w] |= eq[w] & P[b][w] & ~rb;
-      eq[w] &= ~(P[b][w] ^ rb);
-    }
-  }
-  uint32_t m = 0;
-#pragma unroll
-  for (int b = 7; b >= 0; --b) {
-    uint32_t z[NW];
-    uint32_t any = 0;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      z[w] = gt[w] & ~P[b][w];
-      any |= z[w];
-    }
-    const bool one = any == 0u;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) gt[w] = one ? (gt[w] & P[b][w]) : z[w];
-    m |= static_cast<uint32_t>(one) << b;
-  }
-  if (need) hi = m;
+  for (int j = 0; j < BP; ++j) hi[j] = need[j] ? r2[j] : lo[j];
 }
 
-// quantile() of src/chrono.rs:567-579 from its two order statistics: (1-frac)*d[p1] +
-// frac*d[p1+1], or d[k] when the host resolved frac < 0.001 / > 0.999 to a single index.
+// quantile() of src/chrono.rs:567-579 from its order statistics: (1-frac)*d[p1] +
+// frac*d[p1+1], or d[k] alone when the host resolved frac < 0.001 / > 0.999 to one index.
 DEVI float quantile_value(uint32_t lo, uint32_t hi, bool pair, float frac) {
   if (!pair) return static_cast<float>(lo);
   return __fadd_rn(__fmul_rn(__fsub_rn(1.0f, frac), static_cast<float>(lo)),
                    __fmul_rn(frac, static_cast<float>(hi)));
 }
 
-// ---- per-pixel statistics -----------------------------------------------------------------
-template <int C>
-struct PixelStats {
-  // f32 path: median and per-channel factor w*iqr_inv (rel) or w (abs)
-  float med[4][C];
-  float wi[4][C];
-  float q1[4][C];
-  float q3[4][C];
-  // integer path: floor/ceil of the median per channel byte, nh = half-integer medians
-  uint32_t klo[4], khi[4];
-  int nh[4];
-};
-
-// Fill the statistics of the 4 pixels of this thread's column for one word of channel
-// bytes. POS = byte index (0..4C-1) of the first position handled.
-template <int C, int NW, int BP, int KP0>
-DEVI void stats_for_word(const StackDev& S, const RowReader& rd, int w, PixelStats<C>& st,
-                         const uint32_t (&smask)[NW]) {
-  uint32_t P[BP][8][NW];
-  build_planes<C, NW, BP, KP0>(P, rd, w, S.n);
-#pragma unroll
-  for (int k = 0; k < BP; ++k) {
-    const int q = w * 4 + KP0 + k;  // byte within the 4C-byte column
-    const int p = q / C, ch = q % C;
-    if (!((S.wmask >> ch) & 1u)) continue;  // weight 0: median stays 0 (chrono.rs:230, :239)
-    uint32_t lo, hi;
-    select_pair<NW>(P[k], smask, S.med_k, S.med_pair != 0, lo, hi);
-    const float med = S.med_pair ? __fmul_rn(0.5f, __fadd_rn(static_cast<float>(lo),
-                                                             static_cast<float>(hi)))
-                                 : static_cast<float>(lo);
-    st.med[p][ch] = med;
-    const uint32_t s2 = lo + hi;  // 2 * median when paired
-    const uint32_t fl = S.med_pair ? (s2 >> 1) : lo;
-    const uint32_t ce = S.med_pair ? ((s2 + 1) >> 1) : lo;
-    st.klo[p] |= fl << (8 * ch);
-    st.khi[p] |= ce << (8 * ch);
-    st.nh[p] += static_cast<int>(ce - fl);
-    if (!S.thr_abs) {
-      uint32_t a, b;
-      select_pair<NW>(P[k], smask, S.q1_k, S.q1_pair != 0, a, b);
-      const float q1 = quantile_value(a, b, S.q1_pair != 0, S.q1_frac);
-      select_pair<NW>(P[k], smask, S.q3_k, S.q3_pair != 0, a, b);
-      const float q3 = quantile_value(a, b, S.q3_pair != 0, S.q3_frac);
-      st.q1[p][ch] = q1;
-      st.q3[p][ch] = q3;
-      float iqr = __fsub_rn(q3, q1);  // src/chrono.rs:248-252
-      if (iqr == 0.0f) iqr = 1.0f;
-      const float inv = __fdiv_rn(1.0f, iqr);
-      st.wi[p][ch] = __fmul_rn(S.w[ch], inv);
-    } else {
-      st.wi[p][ch] = S.w[ch];
-    }
-  }
-}
-
+// ---- per-pixel arithmetic ------------------------------------------------------------------
 // f32 squared distance of one pixel word to the median, src/chrono.rs:261-279.
 template <int C>
 DEVI float dist_f32(const StackDev& S, const float (&med)[C], const float (&wi)[C], uint32_t px) {
@@ -490,13 +428,6 @@ DEVI uint32_t blend_into_u8(uint32_t a, uint32_t b, float blend) {
 }
 
 template <int NW>
-DEVI int popc_n(const uint32_t (&b)[NW]) {
-  int c = 0;
-#pragma unroll
-  for (int w = 0; w < NW; ++w) c += __popc(b[w]);
-  return c;
-}
-template <int NW>
 DEVI int first_set(const uint32_t (&b)[NW]) {
 #pragma unroll
   for (int w = 0; w < NW; ++w)
@@ -511,288 +442,153 @@ DEVI int last_set(const uint32_t (&b)[NW]) {
   return -1;
 }
 
-// Per-pixel state handed from the distance pass to the epilogue.
-template <int C, int NW>
-struct PixState {
-  uint32_t bits[NW];  // outlier flags, frame i = bit i%32 of word i/32
-  int32_t imax, dmax_i;
-  float dmax_f;
-  uint32_t klo, khi;
-  int32_t nh;
-  float med[C], wi[C], q1[C], q3[C];
-};
 
-// Background, outlier pick and blend of one pixel, src/chrono.rs:290-493, and its
-// diagnostics. Kept out of line and called in a rolled loop to bound code size.
-template <int C, int NW>
-__device__ __noinline__ void pixel_epilogue(const StackDev& S, const RowReader& rd, int p,
-                                            int pix_idx, bool valid, bool fast,
-                                            uint32_t wbytes, const PixState<C, NW>& ps,
-                                            uint32_t& out_pix, uint32_t& out_mask,
-                                            uint32_t& warn_count) {
-  const int n = S.n;
-  auto dsq_of = [&](int f) -> float {  // dist_sq of frame f, recomputed
-    const uint32_t px = load_pixel<C>(rd, f, p);
-    if (fast)
-      return static_cast<float>(dist_int(px, wbytes, ps.klo, ps.khi)) +
-             0.25f * static_cast<float>(ps.nh);
-    return dist_f32<C>(S, ps.med, ps.wi, px);
-  };
-  const int nout = popc_n<NW>(ps.bits);
-  bool warning = false;
-  int bg_idx = -1;
-  uint32_t pix = 0;
-  // background
-  if (S.background == CP_BG_FIRST || S.background == CP_BG_RANDOM) {
-    if (S.background == CP_BG_FIRST) {
-      if (nout == 0) {
-        bg_idx = 0;
-      } else if (nout == n) {
-        bg_idx = 0;
-        warning = true;
-      } else {
-        uint32_t inv[NW];
+// Store the 4 pixel words of a thread (C bytes each) to out at the tile's position: C
+// aligned 32-bit stores for a full, aligned group, else byte stores of the valid pixels.
+template <int C>
+DEVI void store_pixels(uint8_t* out, const TileGeo& g, int tid, const uint32_t (&pw)[4]) {
+  const int first = 4 * tid;
+  if (first >= g.npx) return;
+  uint8_t* dst = out + static_cast<size_t>(g.out_px0 + first) * C;
+  if (first + 4 <= g.npx && (reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
+    uint32_t ow[C];
 #pragma unroll
-        for (int w = 0; w < NW; ++w) inv[w] = ~ps.bits[w];
-        bg_idx = first_set<NW>(inv);  // first_excluded, src/chrono.rs:504-530
-      }
-    } else {
-      const uint64_t pid = static_cast<uint64_t>(pix_idx);
-      if (nout == 0 || nout == n) {
-        bg_idx = static_cast<int>(gen_range(S.seed, pid, static_cast<uint32_t>(n)));
-        warning = nout == n;
-      } else {
-        // sample_excluded, src/chrono.rs:531-555: the j-th outlier (ascending) was swapped
-        // with position n-1-j; trace the drawn position back through the swaps.
-        int pos = static_cast<int>(gen_range(S.seed, pid, static_cast<uint32_t>(n - nout)));
-        int j = nout - 1;
+    for (int i = 0; i < C; ++i) ow[i] = 0u;
 #pragma unroll
-        for (int w = NW - 1; w >= 0; --w) {
-          uint32_t m = ps.bits[w];
-          while (m) {
-            const int bpos = 31 - __clz(m);
-            m &= ~(1u << bpos);
-            const int a = 32 * w + bpos, b = n - 1 - j;
-            if (pos == a)
-              pos = b;
-            else if (pos == b)
-              pos = a;
-            --j;
-          }
-        }
-        bg_idx = pos;
-      }
-    }
-    pix = load_pixel<C>(rd, bg_idx, p);
-  } else if (S.background == CP_BG_AVERAGE) {
-    uint32_t sum[C];
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) sum[ch] = 0u;
-    for (int f = 0; f < n; ++f) {
-      const uint32_t px = load_pixel<C>(rd, f, p);
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) sum[ch] += (px >> (8 * ch)) & 0xFFu;
-    }
-    const float nf = static_cast<float>(n);
-    if (nout == 0) {
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch)
-        pix |= sat_u8(rround(__fdiv_rn(static_cast<float>(sum[ch]), nf))) << (8 * ch);
-    } else {
-      uint32_t osum[C];
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) osum[ch] = 0u;
-#pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        uint32_t m = ps.bits[w];
-        while (m) {
-          const int bpos = __ffs(m) - 1;
-          m &= m - 1;
-          const uint32_t px = load_pixel<C>(rd, 32 * w + bpos, p);
-#pragma unroll
-          for (int ch = 0; ch < C; ++ch) osum[ch] += (px >> (8 * ch)) & 0xFFu;
-        }
-      }
-      // src/chrono.rs:307-333 (the reference's own formula, incl. k = n -> inf)
-      const float ratio = __fdiv_rn(nf, static_cast<float>(n - nout));
+    for (int p = 0; p < 4; ++p)
 #pragma unroll
       for (int ch = 0; ch < C; ++ch) {
-        const float mean = __fdiv_rn(static_cast<float>(sum[ch]), nf);
-        const float v = __fsub_rn(__fmul_rn(mean, ratio),
-                                  __fdiv_rn(static_cast<float>(osum[ch]), nf));
-        pix |= sat_u8(rround(v)) << (8 * ch);
+        const int q = p * C + ch;
+        ow[q / 4] |= ((pw[p] >> (8 * ch)) & 0xFFu) << (8 * (q % 4));
       }
+    uint32_t* o32 = reinterpret_cast<uint32_t*>(dst);
+#pragma unroll
+    for (int i = 0; i < C; ++i) o32[i] = ow[i];
+  } else {
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      if (first + p >= g.npx) break;
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) dst[p * C + ch] = static_cast<uint8_t>(pw[p] >> (8 * ch));
     }
-  } else {  // median (outliers included), src/chrono.rs:340-345
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(ps.med[ch])) << (8 * ch);
-  }
-
-  // outlier pick and blend
-  float blend = 0.0f;
-  int chosen = -1;
-  uint32_t mask = 0;
-  if (nout == 1) {
-    const int si = first_set<NW>(ps.bits);
-    const float dsq = dsq_of(si);
-    blend = __fmul_rn(S.fade[si], blend_value(S, __fsqrt_rn(dsq)));
-    pix = blend_into_u8<C>(pix, load_pixel<C>(rd, si, p), blend);
-    mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
-    chosen = si;
-  } else if (nout > 1) {
-    if (S.outlier == CP_OUTLIER_FORWARD || S.outlier == CP_OUTLIER_BACKWARD) {
-      float pf[C];
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((pix >> (8 * ch)) & 0xFFu);
-      float binv = 1.0f;
-      const bool fwd = S.outlier == CP_OUTLIER_FORWARD;
-      // outliers in ascending (forward) or descending (backward) frame order
-      auto blend_one = [&](int f) {
-        const float b = __fmul_rn(S.fade[f], blend_value(S, __fsqrt_rn(dsq_of(f))));
-        const uint32_t s = load_pixel<C>(rd, f, p);
-        // blend_into_f32_u8, src/color.rs:32-44
-        if (b <= 0.0f) {
-        } else if (b >= 1.0f) {
-#pragma unroll
-          for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((s >> (8 * ch)) & 0xFFu);
-        } else {
-#pragma unroll
-          for (int ch = 0; ch < C; ++ch) {
-            const float sv = static_cast<float>((s >> (8 * ch)) & 0xFFu);
-            pf[ch] = __fadd_rn(pf[ch], __fmul_rn(__fsub_rn(sv, pf[ch]), b));
-          }
-        }
-        binv = __fmul_rn(binv, __fsub_rn(1.0f, b));
-      };
-      if (fwd) {
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-          uint32_t m = ps.bits[w];
-          while (m) {
-            const int f = 32 * w + __ffs(m) - 1;
-            m &= m - 1;
-            blend_one(f);
-          }
-        }
-      } else {
-#pragma unroll
-        for (int w = NW - 1; w >= 0; --w) {
-          uint32_t m = ps.bits[w];
-          while (m) {
-            const int bpos = 31 - __clz(m);
-            m &= ~(1u << bpos);
-            blend_one(32 * w + bpos);
-          }
-        }
-      }
-      pix = 0;
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(pf[ch])) << (8 * ch);
-      mask = sat_u8(rround(__fmul_rn(__fsub_rn(1.0f, binv), 255.0f)));
-      chosen = -2;
-    } else {
-      int si;
-      float dist;
-      uint32_t sample;
-      if (S.outlier == CP_OUTLIER_AVERAGE) {
-        uint32_t osum[C];
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) osum[ch] = 0u;
-        float mdist = 0.0f;
-#pragma unroll
-        for (int w = 0; w < NW; ++w) {
-          uint32_t m = ps.bits[w];
-          while (m) {
-            const int f = 32 * w + __ffs(m) - 1;
-            m &= m - 1;
-            const uint32_t px = load_pixel<C>(rd, f, p);
-#pragma unroll
-            for (int ch = 0; ch < C; ++ch) osum[ch] += (px >> (8 * ch)) & 0xFFu;
-            mdist = __fadd_rn(mdist, __fsqrt_rn(dsq_of(f)));
-          }
-        }
-        const float kf = static_cast<float>(nout);
-        sample = 0;
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch)
-          sample |= sat_u8(rround(__fdiv_rn(static_cast<float>(osum[ch]), kf))) << (8 * ch);
-        si = 0;  // src/chrono.rs:467: the fade of an averaged outlier is taken at frame 0
-        dist = __fdiv_rn(mdist, kf);
-      } else {
-        float dsq;
-        if (S.outlier == CP_OUTLIER_FIRST) {
-          si = first_set<NW>(ps.bits);
-          dsq = dsq_of(si);
-        } else if (S.outlier == CP_OUTLIER_LAST) {
-          si = last_set<NW>(ps.bits);
-          dsq = dsq_of(si);
-        } else {  // extreme
-          si = ps.imax;
-          dsq = fast ? static_cast<float>(ps.dmax_i < 0 ? 0 : ps.dmax_i) +
-                           (ps.dmax_i < 0 ? 0.0f : 0.25f * static_cast<float>(ps.nh))
-                     : ps.dmax_f;
-        }
-        sample = load_pixel<C>(rd, si, p);
-        dist = __fsqrt_rn(dsq);
-      }
-      blend = __fmul_rn(S.fade[si], blend_value(S, dist));
-      pix = blend_into_u8<C>(pix, sample, blend);
-      mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
-      chosen = si;
-    }
-  }
-  out_pix = pix;
-  out_mask = mask;
-  if (valid && warning) warn_count += 1;
-  if (valid) {
-    if (S.dbg_median || S.dbg_q1 || S.dbg_q3) {
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) {
-        const size_t o = static_cast<size_t>(pix_idx) * C + ch;
-        if (S.dbg_median) S.dbg_median[o] = ps.med[ch];
-        if (S.dbg_q1) S.dbg_q1[o] = ps.q1[ch];
-        if (S.dbg_q3) S.dbg_q3[o] = ps.q3[ch];
-      }
-    }
-    if (S.dbg_bits) {
-      const int words = (n + 31) / 32;
-#pragma unroll
-      for (int w = 0; w < NW; ++w)
-        if (w < words) S.dbg_bits[static_cast<size_t>(pix_idx) * words + w] = ps.bits[w];
-    }
-    if (S.dbg_chosen) S.dbg_chosen[pix_idx] = chosen;
-    if (S.dbg_bg) S.dbg_bg[pix_idx] = bg_idx;
-    if (S.dbg_nout) S.dbg_nout[pix_idx] = nout;
   }
 }
 
 // ---- the outlier tile -----------------------------------------------------------------------
-template <int C, int NW>
-__device__ __noinline__ void outlier_tile(const StackDev& S, const TileGeo& g,
-                                          const RowReader& rd, uint32_t& warn_count) {
-  constexpr int BP = NW <= 2 ? 4 : 2;
+template <int C, int NW, bool SH>
+DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
+                       uint32_t& warn_count) {
+  constexpr int BP = NW <= 2 ? 4 : 2;  // byte positions per plane build (register budget)
+  constexpr int NPOS = 4 * C;          // channel bytes of this thread's 4 pixels
+  constexpr int NCH = NPOS / BP;
   const int n = S.n;
-  PixelStats<C> st;
-#pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    st.klo[p] = st.khi[p] = 0u;
-    st.nh[p] = 0;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) st.med[p][ch] = st.wi[p][ch] = st.q1[p][ch] = st.q3[p][ch] = 0.0f;
-  }
+  const int tid = static_cast<int>(threadIdx.x);
   uint32_t smask[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
+  const bool rel = !S.thr_abs;
 
-  // (2)+(3) planes and order statistics, word by word
+  // (2)+(3): planes and order statistics, BP positions per round. Results are shifted into
+  // byte (and float) shift registers so that the rolled loop needs no indexed registers.
+  uint32_t lo_sr[C], hi_sr[C];
+  float wi_sr[NPOS];
 #pragma unroll
-  for (int w = 0; w < C; ++w) {
-    if constexpr (BP == 4) {
-      stats_for_word<C, NW, 4, 0>(S, rd, w, st, smask);
-    } else {
-      stats_for_word<C, NW, 2, 0>(S, rd, w, st, smask);
-      stats_for_word<C, NW, 2, 2>(S, rd, w, st, smask);
+  for (int i = 0; i < C; ++i) lo_sr[i] = hi_sr[i] = 0u;
+#pragma unroll
+  for (int i = 0; i < NPOS; ++i) wi_sr[i] = 0.0f;
+#pragma unroll 1
+  for (int chunk = 0; chunk < NCH; ++chunk) {
+    const int w = (chunk * BP) >> 2, kp0 = (chunk * BP) & 3;
+    uint32_t P[BP][8][NW];
+    build_planes<C, NW, BP, SH>(P, rd, w, kp0, n);
+    uint32_t lo[BP], hi[BP];
+    select_multi<NW, BP>(P, smask, S.med_k, S.med_pair != 0, lo, hi);
+    uint32_t plo = 0, phi = 0;
+#pragma unroll
+    for (int k = 0; k < BP; ++k) {
+      plo |= lo[k] << (8 * k);
+      phi |= hi[k] << (8 * k);
     }
+    if constexpr (BP == 4) {
+#pragma unroll
+      for (int i = 0; i + 1 < C; ++i) {
+        lo_sr[i] = lo_sr[i + 1];
+        hi_sr[i] = hi_sr[i + 1];
+      }
+      lo_sr[C - 1] = plo;
+      hi_sr[C - 1] = phi;
+    } else {
+#pragma unroll
+      for (int i = 0; i + 1 < C; ++i) {
+        lo_sr[i] = __funnelshift_r(lo_sr[i], lo_sr[i + 1], 16);
+        hi_sr[i] = __funnelshift_r(hi_sr[i], hi_sr[i + 1], 16);
+      }
+      lo_sr[C - 1] = (lo_sr[C - 1] >> 16) | (plo << 16);
+      hi_sr[C - 1] = (hi_sr[C - 1] >> 16) | (phi << 16);
+    }
+    if (rel) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
+      uint32_t a1[BP], b1[BP], a3[BP], b3[BP];
+      select_multi<NW, BP>(P, smask, S.q1_k, S.q1_pair != 0, a1, b1);
+      select_multi<NW, BP>(P, smask, S.q3_k, S.q3_pair != 0, a3, b3);
+      float wnew[BP];
+#pragma unroll
+      for (int k = 0; k < BP; ++k) {
+        const float q1 = quantile_value(a1[k], b1[k], S.q1_pair != 0, S.q1_frac);
+        const float q3 = quantile_value(a3[k], b3[k], S.q3_pair != 0, S.q3_frac);
+        float iqr = __fsub_rn(q3, q1);
+        if (iqr == 0.0f) iqr = 1.0f;
+        const int q = chunk * BP + k, ch = q % C;
+        wnew[k] = __fmul_rn(S.w[ch], __fdiv_rn(1.0f, iqr));
+        const int px = g.out_px0 + 4 * tid + q / C;
+        if ((S.dbg_q1 || S.dbg_q3) && 4 * tid + q / C < g.npx) {
+          const bool wt = (S.wmask >> ch) & 1u;
+          if (S.dbg_q1) S.dbg_q1[static_cast<size_t>(px) * C + ch] = wt ? q1 : 0.0f;
+          if (S.dbg_q3) S.dbg_q3[static_cast<size_t>(px) * C + ch] = wt ? q3 : 0.0f;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i + BP < NPOS; ++i) wi_sr[i] = wi_sr[i + BP];
+#pragma unroll
+      for (int k = 0; k < BP; ++k) wi_sr[NPOS - BP + k] = wnew[k];
+    }
+  }
+
+  // per-pixel statistics from the shift registers (compile-time positions)
+  uint32_t klo[4], khi[4];
+  int nh[4];
+  float med[4][C], wi[4][C];
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    klo[p] = khi[p] = 0u;
+    nh[p] = 0;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) {
+      const int q = p * C + ch;
+      const uint32_t lo = (lo_sr[q >> 2] >> (8 * (q & 3))) & 0xFFu;
+      const uint32_t hi = (hi_sr[q >> 2] >> (8 * (q & 3))) & 0xFFu;
+      const bool wt = (S.wmask >> ch) & 1u;
+      // median(), src/chrono.rs:582-591; weight-0 channels keep 0 (chrono.rs:222, :239)
+      med[p][ch] = !wt ? 0.0f
+                       : (S.med_pair ? __fmul_rn(0.5f, __fadd_rn(static_cast<float>(lo),
+                                                                 static_cast<float>(hi)))
+                                     : static_cast<float>(lo));
+      wi[p][ch] = rel ? wi_sr[q] : S.w[ch];
+      const uint32_t s2 = lo + hi;
+      const uint32_t fl = S.med_pair ? (s2 >> 1) : lo, ce = S.med_pair ? ((s2 + 1) >> 1) : lo;
+      if (wt) {
+        klo[p] |= fl << (8 * ch);
+        khi[p] |= ce << (8 * ch);
+        nh[p] += static_cast<int>(ce - fl);
+      }
+    }
+  }
+  if (S.dbg_median) {
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+      if (4 * tid + p < g.npx)
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch)
+          S.dbg_median[static_cast<size_t>(g.out_px0 + 4 * tid + p) * C + ch] = med[p][ch];
   }
 
   // (4) distance pass over all frames (src/chrono.rs:261-288)
@@ -806,12 +602,16 @@ __device__ __noinline__ void outlier_tile(const StackDev& S, const TileGeo& g,
   int32_t dmax_i[4];
   float dmax_f[4];
   int32_t thr_i[4];
+  int32_t kmax[4];
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
     imax[p] = 0;
-    dmax_i[p] = st.nh[p] > 0 ? -1 : 0;  // dist_sq > 0.0 <=> 4D' + nh > 0
+    dmax_i[p] = 0;
+    // max key (D' << 8) + 255 - f; the reference starts from dist_sq 0.0 at frame 0 and
+    // takes strictly larger values: with nh > 0 every frame beats that start (-1)
+    kmax[p] = nh[p] > 0 ? -1 : 255;
     dmax_f[p] = 0.0f;
-    thr_i[p] = S.thr_int[st.nh[p]];
+    thr_i[p] = S.thr_int[nh[p]];
 #pragma unroll
     for (int w = 0; w < NW; ++w) bits[p][w] = 0u;
   }
@@ -821,193 +621,390 @@ __device__ __noinline__ void outlier_tile(const StackDev& S, const TileGeo& g,
     const int fend = min(n, f0 + 32);
     uint32_t ob[4] = {0u, 0u, 0u, 0u};
     if (fast) {
+#pragma unroll 2
       for (int f = f0; f < fend; ++f) {
         uint32_t wv[C];
-#pragma unroll
-        for (int i = 0; i < C; ++i) wv[i] = rd.word(f, i);
+        rd.frame(f, wv);
+        const uint32_t m = 1u << (f - f0);
+        const int32_t fk = 255 - f;
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
           const int32_t d =
-              static_cast<int32_t>(dist_int(pixel_word<C>(wv, p), wbytes, st.klo[p], st.khi[p]));
-          const bool o = d >= thr_i[p];
-          ob[p] |= static_cast<uint32_t>(o) << (f - f0);
-          if (o && d > dmax_i[p]) {
-            dmax_i[p] = d;
-            imax[p] = f;
-          }
+              static_cast<int32_t>(dist_int(pixel_word<C>(wv, p), wbytes, klo[p], khi[p]));
+          ob[p] |= d >= thr_i[p] ? m : 0u;
+          // the largest distance, earliest frame first: the argmax over all frames is an
+          // outlier whenever any frame is one (src/chrono.rs:283-286)
+          kmax[p] = max(kmax[p], (d << 8) + fk);
         }
       }
     } else {
       for (int f = f0; f < fend; ++f) {
         uint32_t wv[C];
-#pragma unroll
-        for (int i = 0; i < C; ++i) wv[i] = rd.word(f, i);
+        rd.frame(f, wv);
+        const uint32_t m = 1u << (f - f0);
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
-          const float d = dist_f32<C>(S, st.med[p], st.wi[p], pixel_word<C>(wv, p));
+          const float d = dist_f32<C>(S, med[p], wi[p], pixel_word<C>(wv, p));
           const bool o = d >= S.thr_sq;
-          ob[p] |= static_cast<uint32_t>(o) << (f - f0);
-          if (o && d > dmax_f[p]) {
-            dmax_f[p] = d;
-            imax[p] = f;
-          }
+          ob[p] |= o ? m : 0u;
+          const bool up = o && d > dmax_f[p];
+          dmax_f[p] = up ? d : dmax_f[p];
+          imax[p] = up ? f : imax[p];
         }
       }
     }
 #pragma unroll
     for (int p = 0; p < 4; ++p) bits[p][blk] = ob[p];
   }
-
-  // (5) per-pixel epilogue
-  PixState<C, NW> ps[4];
-#pragma unroll
-  for (int p = 0; p < 4; ++p) {
-#pragma unroll
-    for (int w = 0; w < NW; ++w) ps[p].bits[w] = bits[p][w];
-    ps[p].imax = imax[p];
-    ps[p].dmax_i = dmax_i[p];
-    ps[p].dmax_f = dmax_f[p];
-    ps[p].klo = st.klo[p];
-    ps[p].khi = st.khi[p];
-    ps[p].nh = st.nh[p];
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) {
-      ps[p].med[ch] = st.med[p][ch];
-      ps[p].wi[ch] = st.wi[p][ch];
-      ps[p].q1[ch] = st.q1[p][ch];
-      ps[p].q3[ch] = st.q3[p][ch];
-    }
-  }
-  uint32_t outw[4], maskb[4];
-#pragma unroll 1
-  for (int p = 0; p < 4; ++p) {
-    const int pix_idx = g.out_px0 + 4 * static_cast<int>(threadIdx.x) + p;
-    const bool valid = 4 * static_cast<int>(threadIdx.x) + p < g.npx;
-    pixel_epilogue<C, NW>(S, rd, p, pix_idx, valid, fast, wbytes, ps[p], outw[p], maskb[p],
-                          warn_count);
-  }
-
-  // output: composite and blend mask (255 in channels >= 3), src/chrono.rs:183-191
-  const int first = 4 * threadIdx.x;
-  if (first >= g.npx) return;
-  const size_t obyte = static_cast<size_t>(g.out_px0 + first) * C;
-  uint32_t bm[4];
-#pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    uint32_t v = 0;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) v |= (ch < 3 ? maskb[p] : 255u) << (8 * ch);
-    bm[p] = v;
-  }
-  const bool aligned = ((reinterpret_cast<uintptr_t>(S.out + obyte) |
-                        (S.blend ? reinterpret_cast<uintptr_t>(S.blend + obyte) : 0)) & 3) == 0;
-  if (first + 4 <= g.npx && aligned) {
-    // 4 pixels = C words
-    uint32_t ow[C], mw[C];
-#pragma unroll
-    for (int i = 0; i < C; ++i) ow[i] = mw[i] = 0u;
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) {
-        const int q = p * C + ch;
-        ow[q / 4] |= ((outw[p] >> (8 * ch)) & 0xFFu) << (8 * (q % 4));
-        mw[q / 4] |= ((bm[p] >> (8 * ch)) & 0xFFu) << (8 * (q % 4));
-      }
-    uint32_t* o32 = reinterpret_cast<uint32_t*>(S.out + obyte);
-#pragma unroll
-    for (int i = 0; i < C; ++i) o32[i] = ow[i];
-    if (S.blend) {
-      uint32_t* b32 = reinterpret_cast<uint32_t*>(S.blend + obyte);
-#pragma unroll
-      for (int i = 0; i < C; ++i) b32[i] = mw[i];
-    }
-  } else {
+  if (fast) {
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
-      if (first + p >= g.npx) break;
+      dmax_i[p] = kmax[p] < 0 ? -1 : (kmax[p] >> 8);
+      imax[p] = kmax[p] < 0 ? 0 : 255 - (kmax[p] & 255);
+    }
+  }
+
+  // (5) per-pixel epilogue, src/chrono.rs:290-493, rolled over the 4 pixels
+  uint32_t outw[4] = {0u, 0u, 0u, 0u}, maskb[4] = {0u, 0u, 0u, 0u};
+#pragma unroll 1
+  for (int p = 0; p < 4; ++p) {
+    const int pix_idx = g.out_px0 + 4 * tid + p;
+    const bool valid = 4 * tid + p < g.npx;
+    uint32_t pb[NW];
 #pragma unroll
-      for (int ch = 0; ch < C; ++ch) {
-        S.out[obyte + p * C + ch] = static_cast<uint8_t>(outw[p] >> (8 * ch));
-        if (S.blend) S.blend[obyte + p * C + ch] = static_cast<uint8_t>(bm[p] >> (8 * ch));
+    for (int w = 0; w < NW; ++w) {
+      uint32_t v = bits[0][w];
+      v = p == 1 ? bits[1][w] : v;
+      v = p == 2 ? bits[2][w] : v;
+      v = p == 3 ? bits[3][w] : v;
+      pb[w] = v;
+    }
+    const uint32_t pklo = pick4(klo, p), pkhi = pick4(khi, p);
+    const int pnh = pick4(nh, p);
+    float pmed[C], pwi[C];
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) {
+      float m = med[0][ch], q = wi[0][ch];
+      m = p == 1 ? med[1][ch] : m;
+      m = p == 2 ? med[2][ch] : m;
+      m = p == 3 ? med[3][ch] : m;
+      q = p == 1 ? wi[1][ch] : q;
+      q = p == 2 ? wi[2][ch] : q;
+      q = p == 3 ? wi[3][ch] : q;
+      pmed[ch] = m;
+      pwi[ch] = q;
+    }
+    auto dsq_of = [&](int f) -> float {  // dist_sq of frame f, recomputed
+      const uint32_t px = load_pixel<C, SH>(rd, f, p);
+      if (fast)
+        return static_cast<float>(dist_int(px, wbytes, pklo, pkhi)) +
+               0.25f * static_cast<float>(pnh);
+      return dist_f32<C>(S, pmed, pwi, px);
+    };
+    int nout = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) nout += __popc(pb[w]);
+    bool warning = false;
+    int bg_idx = -1;
+    uint32_t pix = 0;
+    // background, src/chrono.rs:293-375
+    if (S.background == CP_BG_FIRST || S.background == CP_BG_RANDOM) {
+      if (S.background == CP_BG_FIRST) {
+        if (nout == 0) {
+          bg_idx = 0;
+        } else if (nout == n) {
+          bg_idx = 0;
+          warning = true;
+        } else {
+          uint32_t inv[NW];
+#pragma unroll
+          for (int w = 0; w < NW; ++w) inv[w] = ~pb[w];
+          bg_idx = first_set<NW>(inv);  // first_excluded, src/chrono.rs:504-530
+        }
+      } else {
+        const uint64_t pid = static_cast<uint64_t>(pix_idx);
+        if (nout == 0 || nout == n) {
+          bg_idx = static_cast<int>(gen_range(S.seed, pid, static_cast<uint32_t>(n)));
+          warning = nout == n;
+        } else {
+          // sample_excluded, src/chrono.rs:531-555: the j-th outlier (ascending) was swapped
+          // with position n-1-j; trace the drawn position back through the swaps.
+          int pos = static_cast<int>(gen_range(S.seed, pid, static_cast<uint32_t>(n - nout)));
+          int j = nout - 1;
+#pragma unroll
+          for (int w = NW - 1; w >= 0; --w) {
+            uint32_t m = pb[w];
+            while (m) {
+              const int bpos = 31 - __clz(m);
+              m &= ~(1u << bpos);
+              const int a = 32 * w + bpos, b = n - 1 - j;
+              if (pos == a)
+                pos = b;
+              else if (pos == b)
+                pos = a;
+              --j;
+            }
+          }
+          bg_idx = pos;
+        }
+      }
+      pix = load_pixel<C, SH>(rd, bg_idx, p);
+    } else if (S.background == CP_BG_AVERAGE) {
+      uint32_t sum[C];
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) sum[ch] = 0u;
+      for (int f = 0; f < n; ++f) {
+        const uint32_t px = load_pixel<C, SH>(rd, f, p);
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) sum[ch] += (px >> (8 * ch)) & 0xFFu;
+      }
+      const float nf = static_cast<float>(n);
+      if (nout == 0) {
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch)
+          pix |= sat_u8(rround(__fdiv_rn(static_cast<float>(sum[ch]), nf))) << (8 * ch);
+      } else {
+        uint32_t osum[C];
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) osum[ch] = 0u;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          uint32_t m = pb[w];
+          while (m) {
+            const int bpos = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t px = load_pixel<C, SH>(rd, 32 * w + bpos, p);
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) osum[ch] += (px >> (8 * ch)) & 0xFFu;
+          }
+        }
+        // src/chrono.rs:307-333 (the reference's own formula, incl. k = n -> inf)
+        const float ratio = __fdiv_rn(nf, static_cast<float>(n - nout));
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+          const float mean = __fdiv_rn(static_cast<float>(sum[ch]), nf);
+          const float v = __fsub_rn(__fmul_rn(mean, ratio),
+                                    __fdiv_rn(static_cast<float>(osum[ch]), nf));
+          pix |= sat_u8(rround(v)) << (8 * ch);
+        }
+      }
+    } else {  // median (outliers included), src/chrono.rs:340-345
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(pmed[ch])) << (8 * ch);
+    }
+
+    // outlier pick and blend, src/chrono.rs:377-493
+    float blend = 0.0f;
+    int chosen = -1;
+    uint32_t mask = 0;
+    if (nout == 1) {
+      const int si = first_set<NW>(pb);
+      blend = __fmul_rn(S.fade[si], blend_value(S, __fsqrt_rn(dsq_of(si))));
+      pix = blend_into_u8<C>(pix, load_pixel<C, SH>(rd, si, p), blend);
+      mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
+      chosen = si;
+    } else if (nout > 1) {
+      if (S.outlier == CP_OUTLIER_FORWARD || S.outlier == CP_OUTLIER_BACKWARD) {
+        float pf[C];
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((pix >> (8 * ch)) & 0xFFu);
+        float binv = 1.0f;
+        auto blend_one = [&](int f) {
+          const float b = __fmul_rn(S.fade[f], blend_value(S, __fsqrt_rn(dsq_of(f))));
+          const uint32_t s = load_pixel<C, SH>(rd, f, p);
+          // blend_into_f32_u8, src/color.rs:32-44
+          if (b <= 0.0f) {
+          } else if (b >= 1.0f) {
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((s >> (8 * ch)) & 0xFFu);
+          } else {
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) {
+              const float sv = static_cast<float>((s >> (8 * ch)) & 0xFFu);
+              pf[ch] = __fadd_rn(pf[ch], __fmul_rn(__fsub_rn(sv, pf[ch]), b));
+            }
+          }
+          binv = __fmul_rn(binv, __fsub_rn(1.0f, b));
+        };
+        if (S.outlier == CP_OUTLIER_FORWARD) {
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {
+            uint32_t m = pb[w];
+            while (m) {
+              const int f = 32 * w + __ffs(m) - 1;
+              m &= m - 1;
+              blend_one(f);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int w = NW - 1; w >= 0; --w) {
+            uint32_t m = pb[w];
+            while (m) {
+              const int bpos = 31 - __clz(m);
+              m &= ~(1u << bpos);
+              blend_one(32 * w + bpos);
+            }
+          }
+        }
+        pix = 0;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(pf[ch])) << (8 * ch);
+        mask = sat_u8(rround(__fmul_rn(__fsub_rn(1.0f, binv), 255.0f)));
+        chosen = -2;
+      } else {
+        int si;
+        float dist;
+        uint32_t sample;
+        if (S.outlier == CP_OUTLIER_AVERAGE) {
+          uint32_t osum[C];
+#pragma unroll
+          for (int ch = 0; ch < C; ++ch) osum[ch] = 0u;
+          float mdist = 0.0f;
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {
+            uint32_t m = pb[w];
+            while (m) {
+              const int f = 32 * w + __ffs(m) - 1;
+              m &= m - 1;
+              const uint32_t px = load_pixel<C, SH>(rd, f, p);
+#pragma unroll
+              for (int ch = 0; ch < C; ++ch) osum[ch] += (px >> (8 * ch)) & 0xFFu;
+              mdist = __fadd_rn(mdist, __fsqrt_rn(dsq_of(f)));
+            }
+          }
+          const float kf = static_cast<float>(nout);
+          sample = 0;
+#pragma unroll
+          for (int ch = 0; ch < C; ++ch)
+            sample |= sat_u8(rround(__fdiv_rn(static_cast<float>(osum[ch]), kf))) << (8 * ch);
+          si = 0;  // src/chrono.rs:467: the fade of an averaged outlier is taken at frame 0
+          dist = __fdiv_rn(mdist, kf);
+        } else {
+          float dsq;
+          if (S.outlier == CP_OUTLIER_FIRST) {
+            si = first_set<NW>(pb);
+            dsq = dsq_of(si);
+          } else if (S.outlier == CP_OUTLIER_LAST) {
+            si = last_set<NW>(pb);
+            dsq = dsq_of(si);
+          } else {  // extreme
+            si = pick4(imax, p);
+            if (fast) {
+              const int32_t dm = pick4(dmax_i, p);
+              dsq = dm < 0 ? 0.0f
+                           : static_cast<float>(dm) + 0.25f * static_cast<float>(pnh);
+            } else {
+              dsq = pick4(dmax_f, p);
+            }
+          }
+          sample = load_pixel<C, SH>(rd, si, p);
+          dist = __fsqrt_rn(dsq);
+        }
+        blend = __fmul_rn(S.fade[si], blend_value(S, dist));
+        pix = blend_into_u8<C>(pix, sample, blend);
+        mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
+        chosen = si;
       }
     }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      outw[q] = q == p ? pix : outw[q];
+      maskb[q] = q == p ? mask : maskb[q];
+    }
+    if (valid) {
+      if (warning) warn_count += 1;
+      if (S.dbg_bits) {
+        const int words = (n + 31) / 32;
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+          if (w < words) S.dbg_bits[static_cast<size_t>(pix_idx) * words + w] = pb[w];
+      }
+      if (S.dbg_chosen) S.dbg_chosen[pix_idx] = chosen;
+      if (S.dbg_bg) S.dbg_bg[pix_idx] = bg_idx;
+      if (S.dbg_nout) S.dbg_nout[pix_idx] = nout;
+    }
+  }
+  store_pixels<C>(S.out, g, tid, outw);
+  if (S.blend) {
+    uint32_t bm[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) v |= (ch < 3 ? maskb[p] : 255u) << (8 * ch);
+      bm[p] = v;
+    }
+    store_pixels<C>(S.blend, g, tid, bm);  // blend mask, 255 in channels >= 3 (chrono.rs:183-191)
   }
 }
 
 // ---- darker / lighter tile ----------------------------------------------------------------
 // SimpleProcessor fold, src/simple.rs:96-133: running extreme of sum_c p_c * w_c (f32, c
 // ascending, strict compare: the earliest frame wins ties); on a new extreme the frame's
-// pixel is blended into the running output (starting at 0) with the fade.
-template <int C>
-__device__ __noinline__ void simple_tile(const StackDev& S, const TileGeo& g,
-                                         const RowReader& rd) {
+// pixel is blended into the running output (starting at 0) with the frame's fade.
+template <int C, bool SH>
+DEVI void simple_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd) {
   const bool darker = S.mode == CP_MODE_DARKER;
-  float ext[4];
-  uint32_t outw[4];
+  const int tid = static_cast<int>(threadIdx.x);
+  uint32_t outw[4] = {0u, 0u, 0u, 0u};
+  if (S.unit_w && S.no_fade) {
+    // weights 0/1: the f32 sum is an exact integer; every fade is >= 1: copy on a new extreme
+    uint32_t wbytes = 0;
 #pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    ext[p] = darker ? FLT_MAX : -FLT_MAX;
-    outw[p] = 0u;
-  }
-  for (int f = 0; f < S.n; ++f) {
-    uint32_t wv[C];
+    for (int ch = 0; ch < C; ++ch)
+      if ((S.wmask >> ch) & 1u) wbytes |= 0xFFu << (8 * ch);
+    int32_t ext[4];
 #pragma unroll
-    for (int i = 0; i < C; ++i) wv[i] = rd.word(f, i);
-    const float fade = S.fade[f];
+    for (int p = 0; p < 4; ++p) ext[p] = darker ? 0x7FFFFFFF : -1;
+#pragma unroll 4
+    for (int f = 0; f < S.n; ++f) {
+      uint32_t wv[C];
+      rd.frame(f, wv);
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      const uint32_t px = pixel_word<C>(wv, p);
-      float value = 0.0f;
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch)
-        value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
-      const bool is_ext = darker ? (value < ext[p]) : (value > ext[p]);
-      if (is_ext) {
-        ext[p] = value;
-        if (fade > 0.0f) outw[p] = fade >= 1.0f ? px : blend_into_u8<C>(outw[p], px, fade);
+      for (int p = 0; p < 4; ++p) {
+        const uint32_t px = pixel_word<C>(wv, p);
+        const int32_t v = static_cast<int32_t>(__dp4a(px & wbytes, 0x01010101u, 0u));
+        const bool up = darker ? v < ext[p] : v > ext[p];
+        ext[p] = up ? v : ext[p];
+        outw[p] = up ? px : outw[p];
       }
     }
-  }
-  const int first = 4 * threadIdx.x;
-  if (first >= g.npx) return;
-  const size_t obyte = static_cast<size_t>(g.out_px0 + first) * C;
-  if (first + 4 <= g.npx && (reinterpret_cast<uintptr_t>(S.out + obyte) & 3) == 0) {
-    uint32_t ow[C];
-#pragma unroll
-    for (int i = 0; i < C; ++i) ow[i] = 0u;
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) {
-        const int q = p * C + ch;
-        ow[q / 4] |= ((outw[p] >> (8 * ch)) & 0xFFu) << (8 * (q % 4));
-      }
-    uint32_t* o32 = reinterpret_cast<uint32_t*>(S.out + obyte);
-#pragma unroll
-    for (int i = 0; i < C; ++i) o32[i] = ow[i];
   } else {
+    float ext[4];
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      if (first + p >= g.npx) break;
+    for (int p = 0; p < 4; ++p) ext[p] = darker ? FLT_MAX : -FLT_MAX;
+    for (int f = 0; f < S.n; ++f) {
+      uint32_t wv[C];
+      rd.frame(f, wv);
+      const float fade = S.fade[f];
 #pragma unroll
-      for (int ch = 0; ch < C; ++ch)
-        S.out[obyte + p * C + ch] = static_cast<uint8_t>(outw[p] >> (8 * ch));
+      for (int p = 0; p < 4; ++p) {
+        const uint32_t px = pixel_word<C>(wv, p);
+        float value = 0.0f;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch)
+          value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
+        const bool up = darker ? (value < ext[p]) : (value > ext[p]);
+        ext[p] = up ? value : ext[p];
+        if (up && fade > 0.0f) outw[p] = fade >= 1.0f ? px : blend_into_u8<C>(outw[p], px, fade);
+      }
     }
   }
+  store_pixels<C>(S.out, g, tid, outw);
 }
 
-template <int C>
-DEVI void process_tile(const StackDev& S, const TileGeo& g, const RowReader& rd,
+template <int C, bool SH>
+DEVI void process_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
                        uint32_t& warn) {
   if (S.mode != CP_MODE_OUTLIER) {
-    simple_tile<C>(S, g, rd);
+    simple_tile<C, SH>(S, g, rd);
   } else if (S.nw == 1) {
-    outlier_tile<C, 1>(S, g, rd, warn);
+    outlier_tile<C, 1, SH>(S, g, rd, warn);
   } else if (S.nw == 2) {
-    outlier_tile<C, 2>(S, g, rd, warn);
+    outlier_tile<C, 2, SH>(S, g, rd, warn);
   } else {
-    outlier_tile<C, 4>(S, g, rd, warn);
+    outlier_tile<C, 4, SH>(S, g, rd, warn);
   }
 }
 
@@ -1030,9 +1027,36 @@ DEVI SmemLayout smem_layout(uint8_t* smem) {
   return l;
 }
 
+// Stage a tile, wait for it (bounded) and process it. Returns false after a timed-out wait.
+template <int C>
+DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uint32_t& phase,
+                   uint32_t* error, uint32_t& warn) {
+  if (threadIdx.x < 32) {
+    fence_proxy_async();
+    issue_tile<C>(S, g, L.buf, L.shifts, L.bar);
+  }
+  __syncthreads();
+  if (!mbar_wait(L.bar, phase)) {
+    if (error) atomicOr(error, 1u);
+    return false;
+  }
+  phase ^= 1u;
+  const uint8_t* col = L.buf + 4 * C * threadIdx.x;
+  if (S.shifted) {
+    const Rows<C, true> rd{col, L.shifts};
+    process_tile<C, true>(S, g, rd, warn);
+  } else {
+    const Rows<C, false> rd{col, L.shifts};
+    process_tile<C, false>(S, g, rd, warn);
+  }
+  __syncthreads();
+  return true;
+}
+
 // One stack, persistent CTAs striding over its tiles.
 template <int C>
-__global__ void __launch_bounds__(kThreads) k_composite(const __grid_constant__ StackDev S, uint32_t* error) {
+__global__ void __launch_bounds__(kThreads) k_composite(const __grid_constant__ StackDev S,
+                                                        uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
   const SmemLayout L = smem_layout(smem);
   if (threadIdx.x == 0) {
@@ -1040,33 +1064,18 @@ __global__ void __launch_bounds__(kThreads) k_composite(const __grid_constant__ 
     fence_mbar_init();
   }
   __syncthreads();
-  const int pitch = row_pitch(S.tile_px, C);
-  const RowReader rd{L.buf, L.shifts, pitch, 4 * C * static_cast<int>(threadIdx.x), S.shifted != 0};
   uint32_t phase = 0, warn = 0;
-  for (int t = blockIdx.x; t < S.tiles; t += gridDim.x) {
-    const TileGeo g = tile_geo(S, t);
-    if (threadIdx.x < 32) {
-      fence_proxy_async();
-      issue_tile<C>(S, g, L.buf, pitch, L.shifts, L.bar);
-    }
-    __syncthreads();
-    if (!mbar_wait(L.bar, phase)) {
-      if (error) atomicOr(error, 1u);
-      return;
-    }
-    phase ^= 1u;
-    process_tile<C>(S, g, rd, warn);
-    __syncthreads();
-  }
+  for (int t = blockIdx.x; t < S.tiles; t += gridDim.x)
+    if (!run_tile<C>(S, tile_geo(S, t), L, phase, error, warn)) return;
   flush_warnings(S.warnings, warn);
 }
 
 // Many stacks: persistent CTAs pull (stack, tile) items from a device counter.
 template <int C>
 __global__ void __launch_bounds__(kThreads) k_composite_batch(const StackDev* __restrict__ stacks,
-                                                        const int32_t* __restrict__ prefix,
-                                                        int32_t n_stacks, int32_t total,
-                                                        uint32_t* counter, uint32_t* error) {
+                                                              const int32_t* __restrict__ prefix,
+                                                              int32_t n_stacks, int32_t total,
+                                                              uint32_t* counter, uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ int item_s, stack_s;
   const SmemLayout L = smem_layout(smem);
@@ -1091,23 +1100,135 @@ __global__ void __launch_bounds__(kThreads) k_composite_batch(const StackDev* __
     const int it = item_s, s = stack_s;
     if (it >= total) break;
     const StackDev& S = stacks[s];
-    const int pitch = row_pitch(S.tile_px, C);
-    const TileGeo g = tile_geo(S, it - prefix[s]);
-    if (threadIdx.x < 32) {
-      fence_proxy_async();
-      issue_tile<C>(S, g, L.buf, pitch, L.shifts, L.bar);
-    }
-    __syncthreads();
-    if (!mbar_wait(L.bar, phase)) {
-      if (error) atomicOr(error, 1u);
-      return;
-    }
-    phase ^= 1u;
-    const RowReader rd{L.buf, L.shifts, pitch, 4 * C * static_cast<int>(threadIdx.x), S.shifted != 0};
     uint32_t warn = 0;
-    if (static_cast<int>(threadIdx.x) < S.threads) process_tile<C>(S, g, rd, warn);
+    if (!run_tile<C>(S, tile_geo(S, it - prefix[s]), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
-    __syncthreads();
+  }
+}
+
+
+// darker/lighter streaming over an aligned, uncropped stack (no shared-memory staging): each
+// thread owns 16 pixels, i.e. C 16-byte words of every frame, and folds its frames in order
+// with 128-bit loads, four frames in flight. FAST: weights 0/1 and every fade >= 1, where the
+// f32 sum of src/simple.rs:103-106 is an exact integer and a new extreme copies the pixel.
+template <int C, bool FAST>
+__global__ void __launch_bounds__(256) k_simple_stream(const __grid_constant__ StackDev S) {
+  constexpr int NWD = 4 * C;  // 32-bit words per thread per frame
+  const bool darker = S.mode == CP_MODE_DARKER;
+  const int groups = (S.px_end - S.px_begin) / 16;
+  const int tail = (S.px_end - S.px_begin) - 16 * groups;
+  const int n = S.n;
+  uint32_t wbytes = 0;
+#pragma unroll
+  for (int ch = 0; ch < C; ++ch)
+    if ((S.wmask >> ch) & 1u) wbytes |= 0xFFu << (8 * ch);
+  const int stride = gridDim.x * blockDim.x;
+  for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < groups + tail; gi += stride) {
+    if (gi >= groups) {  // tail pixels one by one
+      const size_t o = static_cast<size_t>(S.px_begin + 16 * groups + (gi - groups)) * C;
+      float ext = darker ? FLT_MAX : -FLT_MAX;
+      uint32_t out = 0;
+      for (int f = 0; f < n; ++f) {
+        uint32_t px = 0;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) px |= static_cast<uint32_t>(S.frames[f][o + ch]) << (8 * ch);
+        float value = 0.0f;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch)
+          value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
+        const bool up = darker ? (value < ext) : (value > ext);
+        ext = up ? value : ext;
+        const float fade = S.fade[f];
+        if (up && fade > 0.0f) out = fade >= 1.0f ? px : blend_into_u8<C>(out, px, fade);
+      }
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) S.out[o + ch] = static_cast<uint8_t>(out >> (8 * ch));
+      continue;
+    }
+    const size_t off = static_cast<size_t>(S.px_begin + 16 * gi) * C;
+    int32_t exti[16];
+    float extf[16];
+    uint32_t outw[16];
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+      exti[p] = darker ? 0x7FFFFFFF : -1;
+      extf[p] = darker ? FLT_MAX : -FLT_MAX;
+      outw[p] = 0u;
+    }
+    auto fold = [&](const uint32_t (&wv)[NWD], int f) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        uint32_t sub[C];
+#pragma unroll
+        for (int i = 0; i < C; ++i) sub[i] = wv[q * C + i];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          const int pp = q * 4 + p;
+          const uint32_t px = pixel_word<C>(sub, p);
+          if constexpr (FAST) {
+            const int32_t v = static_cast<int32_t>(__dp4a(px & wbytes, 0x01010101u, 0u));
+            const bool up = darker ? v < exti[pp] : v > exti[pp];
+            exti[pp] = up ? v : exti[pp];
+            outw[pp] = up ? px : outw[pp];
+          } else {
+            float value = 0.0f;
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch)
+              value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
+            const bool up = darker ? (value < extf[pp]) : (value > extf[pp]);
+            extf[pp] = up ? value : extf[pp];
+            const float fade = S.fade[f];
+            if (up && fade > 0.0f)
+              outw[pp] = fade >= 1.0f ? px : blend_into_u8<C>(outw[pp], px, fade);
+          }
+        }
+      }
+    };
+    int f = 0;
+    for (; f + 4 <= n; f += 4) {
+      uint32_t wv[4][NWD];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint4* src = reinterpret_cast<const uint4*>(S.frames[f + j] + off);
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+          const uint4 v = __ldcs(src + i);  // streamed once: evict first
+          wv[j][4 * i] = v.x;
+          wv[j][4 * i + 1] = v.y;
+          wv[j][4 * i + 2] = v.z;
+          wv[j][4 * i + 3] = v.w;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) fold(wv[j], f + j);
+    }
+    for (; f < n; ++f) {
+      uint32_t wv[NWD];
+      const uint4* src = reinterpret_cast<const uint4*>(S.frames[f] + off);
+#pragma unroll
+      for (int i = 0; i < C; ++i) {
+        const uint4 v = __ldcs(src + i);
+        wv[4 * i] = v.x;
+        wv[4 * i + 1] = v.y;
+        wv[4 * i + 2] = v.z;
+        wv[4 * i + 3] = v.w;
+      }
+      fold(wv, f);
+    }
+    // 16 pixels = C 16-byte words
+    uint32_t ow[NWD];
+#pragma unroll
+    for (int i = 0; i < NWD; ++i) ow[i] = 0u;
+#pragma unroll
+    for (int pp = 0; pp < 16; ++pp)
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) {
+        const int b = pp * C + ch;
+        ow[b / 4] |= ((outw[pp] >> (8 * ch)) & 0xFFu) << (8 * (b % 4));
+      }
+    uint4* dst = reinterpret_cast<uint4*>(S.out + off);
+#pragma unroll
+    for (int i = 0; i < C; ++i) dst[i] = make_uint4(ow[4 * i], ow[4 * i + 1], ow[4 * i + 2], ow[4 * i + 3]);
   }
 }
 
