@@ -7,7 +7,7 @@ import ctypes as ct
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libchrono_gpu.so")
+LIB_PATH = os.environ.get("CHRONO_GPU_LIB") or os.path.join(HERE, "lib", "libchrono_gpu.so")
 
 CP_OK = 0
 CP_ERR_ARG = -1
@@ -97,6 +97,9 @@ SIGNATURES = [
                                 ct.POINTER(Debug), U64P]),
     ("cp_composite_batch_device", ct.c_int, [P, ct.POINTER(Stack), ct.POINTER(Params), I32,
                                              ct.POINTER(P), ct.POINTER(P), P, P]),
+    ("cp_composite_video_device", ct.c_int, [P, ct.POINTER(P), I32, I32, I32, I32, I32, I64P,
+                                             I32P, I32P, ct.POINTER(Params), ct.POINTER(P),
+                                             ct.POINTER(P), P, P]),
     ("cp_shake_analyze_device", ct.c_int, [P, ct.POINTER(P), I32, I32, I32, I32, I32P, I32,
                                            I32, I32, I32P, I32P]),
     ("cp_server_create", ct.c_int, [P, U64, I32, ct.POINTER(P)]),

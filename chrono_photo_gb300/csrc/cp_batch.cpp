@@ -48,9 +48,9 @@ static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_
   if (e != cudaSuccess) return cuda_status(ctx, e, "memset");
   int rc = 0;
   switch (channels) {
-    case 1: rc = launch_batch_c1(d_stacks, d_prefix, n_stacks, plan.total, d_counter, ctx->d_error, grid, smem, st); break;
-    case 3: rc = launch_batch_c3(d_stacks, d_prefix, n_stacks, plan.total, d_counter, ctx->d_error, grid, smem, st); break;
-    default: rc = launch_batch_c4(d_stacks, d_prefix, n_stacks, plan.total, d_counter, ctx->d_error, grid, smem, st); break;
+    case 1: rc = launch_batch_c1(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;
+    case 3: rc = launch_batch_c3(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;
+    default: rc = launch_batch_c4(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;
   }
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "batch launch");
 }
@@ -59,10 +59,10 @@ static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_
 
 using namespace cp;
 
-extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
-                                         const cp_params* params, int32_t n_stacks,
-                                         uint8_t* const* outs, uint8_t* const* out_blends,
-                                         uint64_t* warnings, void* stream) {
+// Batch with per-stack warning counters (device pointers, nullable).
+static int batch_run(cp_ctx* ctx, const cp_stack* stacks, const cp_params* params,
+                     int32_t n_stacks, uint8_t* const* outs, uint8_t* const* out_blends,
+                     uint64_t* const* warn_ptrs, void* stream) {
   if (!ctx || !stacks || !params || !outs || n_stacks < 1) return CP_ERR_ARG;
   cudaSetDevice(ctx->device);
   std::vector<StackDev> host(static_cast<size_t>(n_stacks));
@@ -85,7 +85,7 @@ extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
     if (rc) return rc;
     d.out = outs[i];
     d.blend = (out_blends && params[i].mode == CP_MODE_OUTLIER) ? out_blends[i] : nullptr;
-    d.warnings = warnings ? reinterpret_cast<unsigned long long*>(warnings + i) : nullptr;
+    d.warnings = warn_ptrs ? reinterpret_cast<unsigned long long*>(warn_ptrs[i]) : nullptr;
     max_n = std::max(max_n, s.n);
     prefix[static_cast<size_t>(i) + 1] = prefix[static_cast<size_t>(i)] + d.tiles;
   }
@@ -113,6 +113,12 @@ extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
     std::unique_ptr<BatchPlan> np(new BatchPlan());
     np->host = host;
     np->total = prefix.back();
+    np->max_n = max_n;
+    np->interleave = 1;
+    for (const StackDev& d : host)
+      if (d.tiles != host[0].tiles || d.width != host[0].width || d.height != host[0].height ||
+          d.has_crop != host[0].has_crop)
+        np->interleave = 0;
     np->dev_bytes = sizeof(StackDev) * host.size() + sizeof(int32_t) * prefix.size() + 64;
     int rc = dev_alloc(ctx, np->dev_bytes, &np->dev);
     if (rc) return rc;
@@ -152,4 +158,63 @@ extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
     plan = ctx->plans.back().get();
   }
   return cuda_status(ctx, cudaGraphLaunch(plan->exec, st), "graph launch");
+}
+
+extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
+                                         const cp_params* params, int32_t n_stacks,
+                                         uint8_t* const* outs, uint8_t* const* out_blends,
+                                         uint64_t* warnings, void* stream) {
+  if (n_stacks < 1) return CP_ERR_ARG;
+  std::vector<uint64_t*> wp(static_cast<size_t>(n_stacks), nullptr);
+  if (warnings)
+    for (int i = 0; i < n_stacks; ++i) wp[static_cast<size_t>(i)] = warnings + i;
+  return batch_run(ctx, stacks, params, n_stacks, outs, out_blends, warnings ? wp.data() : nullptr,
+                   stream);
+}
+
+extern "C" int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* frames,
+                                         int32_t image_count, int32_t width, int32_t height,
+                                         int32_t channels, int32_t n_windows,
+                                         const int64_t* win_start, const int32_t* win_len,
+                                         const int32_t* win_indices, const cp_params* params,
+                                         uint8_t* const* outs, uint8_t* const* out_blends,
+                                         uint64_t* warnings, void* stream) {
+  // One composite per chrono-video window (src/main.rs:254-330) over frames resident on the
+  // device; windows without frames are skipped, as the reference skips them (:326-328).
+  if (!ctx || !frames || !win_start || !win_len || !win_indices || !params || !outs ||
+      n_windows < 0 || image_count < 1)
+    return CP_ERR_ARG;
+  std::vector<cp_stack> stacks;
+  std::vector<cp_params> ps;
+  std::vector<uint8_t*> o, b;
+  std::vector<uint64_t*> wp;
+  std::vector<std::vector<const uint8_t*>> tables;
+  tables.reserve(static_cast<size_t>(n_windows));
+  for (int k = 0; k < n_windows; ++k) {
+    const int len = win_len[k];
+    if (len <= 0) continue;
+    std::vector<const uint8_t*> t(static_cast<size_t>(len));
+    for (int i = 0; i < len; ++i) {
+      const int idx = win_indices[win_start[k] + i];
+      if (idx < 0 || idx >= image_count) return CP_ERR_ARG;
+      t[static_cast<size_t>(i)] = frames[idx];
+    }
+    tables.push_back(std::move(t));
+    cp_stack s;
+    std::memset(&s, 0, sizeof s);
+    s.n = len;
+    s.width = width;
+    s.height = height;
+    s.channels = channels;
+    s.frames = tables.back().data();
+    s.frame_offset = win_indices[win_start[k]];  // indices[0] (src/chrono.rs:103)
+    stacks.push_back(s);
+    ps.push_back(*params);
+    o.push_back(outs[k]);
+    b.push_back(out_blends ? out_blends[k] : nullptr);
+    wp.push_back(warnings ? warnings + k : nullptr);
+  }
+  if (stacks.empty()) return CP_OK;
+  return batch_run(ctx, stacks.data(), ps.data(), static_cast<int32_t>(stacks.size()), o.data(),
+                   out_blends ? b.data() : nullptr, warnings ? wp.data() : nullptr, stream);
 }

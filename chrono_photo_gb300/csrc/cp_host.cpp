@@ -166,7 +166,7 @@ int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
   d->outlier = p->outlier;
   d->background = p->background;
   d->thr_abs = p->thr_abs ? 1 : 0;
-  bool unit = true, neg = false;
+  bool unit = true, neg = false, finite = true;
   uint32_t wmask = 0;
   for (int c = 0; c < 4; ++c) {
     d->w[c] = p->weights[c];
@@ -174,10 +174,12 @@ int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
     if (c < st->channels && !(p->weights[c] == 0.0f || p->weights[c] == 1.0f)) unit = false;
     if (c < st->channels && std::signbit(p->weights[c]) && p->weights[c] != 0.0f) neg = true;
     if (c < st->channels && std::isnan(p->weights[c])) neg = true;
+    if (c < st->channels && !(std::fabs(p->weights[c]) < 1e30f)) finite = false;
   }
   d->wmask = wmask;
   d->neg_w = neg ? 1u : 0u;
   d->unit_w = unit ? 1u : 0u;
+  d->finite_w = finite ? 1u : 0u;
   d->fast_int = (d->thr_abs && unit) ? 1u : 0u;
   // Threshold::new, src/options.rs:197-213 (f32 arithmetic)
   if (d->thr_abs) {

@@ -32,6 +32,8 @@ struct BatchPlan {
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   int32_t total = 0;
+  int32_t interleave = 0;  // equal-geometry stacks: tile-major work order
+  int32_t max_n = 0;
 };
 
 }  // namespace cp

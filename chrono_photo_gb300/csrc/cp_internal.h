@@ -45,6 +45,7 @@ struct StackDev {
   uint32_t fast_int;   // abs threshold and every weight 0 or 1: exact integer distances
   uint32_t neg_w;      // some weight negative
   uint32_t unit_w;     // every weight 0 or 1
+  uint32_t finite_w;   // every weight finite with |w| < 1e30: w * iqr_inv stays finite
   uint32_t no_fade;    // every fade factor >= 1 (darker/lighter copy the pixel)
   float thr_min, thr_max, thr_scale, thr_sq;
   int32_t thr_int[5];  // smallest integer D' with D' + nh/4 >= thr_sq, per nh = 0..4
@@ -74,8 +75,8 @@ inline int smem_bytes_for(int n, int tile_px, int channels) {
   int launch_composite_c##CH(const StackDev& s, int grid, int smem, void* stream,         \
                              uint32_t* error);                                            \
   int launch_batch_c##CH(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks, \
-                         int32_t total, uint32_t* counter, uint32_t* error, int grid,     \
-                         int smem, void* stream);                                 \
+                         int32_t total, int32_t interleave, uint32_t* counter,            \
+                         uint32_t* error, int grid, int smem, void* stream);              \
   int simple_stream_max_ctas_c##CH(bool fast);                                            \
   int launch_simple_stream_c##CH(const StackDev& s, bool fast, int grid, void* stream);
 CP_DECLARE_CH(1)

@@ -37,6 +37,10 @@ namespace {
 
 constexpr int kSmemHeader = 256;            // mbarrier + per-frame byte shifts
 constexpr long long kWaitCycles = 1ll << 32; // ~2 s at 2 GHz before a wait gives up
+#ifndef CP_DUNROLL
+#define CP_DUNROLL 2
+#endif
+constexpr int kDistUnroll = CP_DUNROLL;        // frames per distance-loop iteration
 
 // ---- PTX wrappers ------------------------------------------------------------------------
 DEVI uint32_t smem_u32(const void* p) {
@@ -351,7 +355,7 @@ DEVI void radix_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], c
 }
 
 // Order statistics d[k] (lo) and, when `pair`, d[k+1] (hi). d[k+1] equals d[k] while the run
-// of equal values continues past rank k; otherwise a second radix select finds it.
+// of equal values continues past rank k; otherwise it is found by a second pass.
 template <int NW, int BP>
 DEVI void select_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], int k,
                        bool pair, uint32_t (&lo)[BP], uint32_t (&hi)[BP]) {
@@ -389,19 +393,24 @@ DEVI float quantile_value(uint32_t lo, uint32_t hi, bool pair, float frac) {
 }
 
 // ---- per-pixel arithmetic ------------------------------------------------------------------
-// f32 squared distance of one pixel word to the median, src/chrono.rs:261-279.
-template <int C>
-DEVI float dist_f32(const StackDev& S, const float (&med)[C], const float (&wi)[C], uint32_t px) {
+// f32 squared distance of one pixel word to the median, src/chrono.rs:261-279, in the
+// reference's operation order. `medo` is median + 2^22: with the sample byte placed in the
+// mantissa of 2^22 (ulp 0.5) both are exact and their difference is exactly median - p.
+// The `diff == 0 -> 0` case needs no select when every w * iqr_inv is finite (FINITE), since
+// then t = wi * 0 = 0 and t * t = 0.
+template <int C, bool FINITE>
+DEVI float dist_f32(const StackDev& S, const float (&medo)[C], const float (&wi)[C], uint32_t px) {
   float d = 0.0f;
 #pragma unroll
   for (int ch = 0; ch < C; ++ch) {
     if ((S.wmask >> ch) & 1u) {
-      const float v = u8f((px >> (8 * ch)) & 0xFFu);
-      const float diff = __fsub_rn(med[ch], v);
+      const float v = __uint_as_float(0x4A800000u + (((px >> (8 * ch)) & 0xFFu) << 1));
+      const float diff = __fsub_rn(medo[ch], v);
       const float t = __fmul_rn(wi[ch], diff);
       float term = __fmul_rn(t, t);
       if (S.neg_w) term = __fmul_rn(rsignum(S.w[ch]), term);
-      d = __fadd_rn(d, diff == 0.0f ? 0.0f : term);
+      if constexpr (!FINITE) term = diff == 0.0f ? 0.0f : term;
+      d = __fadd_rn(d, term);
     }
   }
   return d;
@@ -556,7 +565,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
   // per-pixel statistics from the shift registers (compile-time positions)
   uint32_t klo[4], khi[4];
   int nh[4];
-  float med[4][C], wi[4][C];
+  float med[4][C], medo[4][C], wi[4][C];
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
     klo[p] = khi[p] = 0u;
@@ -572,6 +581,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
                        : (S.med_pair ? __fmul_rn(0.5f, __fadd_rn(static_cast<float>(lo),
                                                                  static_cast<float>(hi)))
                                      : static_cast<float>(lo));
+      medo[p][ch] = __fadd_rn(med[p][ch], 4194304.0f);  // exact: med is a multiple of 1/2
       wi[p][ch] = rel ? wi_sr[q] : S.w[ch];
       const uint32_t s2 = lo + hi;
       const uint32_t fl = S.med_pair ? (s2 >> 1) : lo, ce = S.med_pair ? ((s2 + 1) >> 1) : lo;
@@ -621,7 +631,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     const int fend = min(n, f0 + 32);
     uint32_t ob[4] = {0u, 0u, 0u, 0u};
     if (fast) {
-#pragma unroll 2
+#pragma unroll kDistUnroll
       for (int f = f0; f < fend; ++f) {
         uint32_t wv[C];
         rd.frame(f, wv);
@@ -637,6 +647,21 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
           kmax[p] = max(kmax[p], (d << 8) + fk);
         }
       }
+    } else if (S.finite_w) {
+      for (int f = f0; f < fend; ++f) {
+        uint32_t wv[C];
+        rd.frame(f, wv);
+        const uint32_t m = 1u << (f - f0);
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          const float d = dist_f32<C, true>(S, medo[p], wi[p], pixel_word<C>(wv, p));
+          const bool o = d >= S.thr_sq;
+          ob[p] |= o ? m : 0u;
+          const bool up = o && d > dmax_f[p];
+          dmax_f[p] = up ? d : dmax_f[p];
+          imax[p] = up ? f : imax[p];
+        }
+      }
     } else {
       for (int f = f0; f < fend; ++f) {
         uint32_t wv[C];
@@ -644,7 +669,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
         const uint32_t m = 1u << (f - f0);
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
-          const float d = dist_f32<C>(S, med[p], wi[p], pixel_word<C>(wv, p));
+          const float d = dist_f32<C, false>(S, medo[p], wi[p], pixel_word<C>(wv, p));
           const bool o = d >= S.thr_sq;
           ob[p] |= o ? m : 0u;
           const bool up = o && d > dmax_f[p];
@@ -681,13 +706,17 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     }
     const uint32_t pklo = pick4(klo, p), pkhi = pick4(khi, p);
     const int pnh = pick4(nh, p);
-    float pmed[C], pwi[C];
+    float pmed[C], pmedo[C], pwi[C];
 #pragma unroll
     for (int ch = 0; ch < C; ++ch) {
-      float m = med[0][ch], q = wi[0][ch];
+      float m = med[0][ch], q = wi[0][ch], mo = medo[0][ch];
       m = p == 1 ? med[1][ch] : m;
       m = p == 2 ? med[2][ch] : m;
       m = p == 3 ? med[3][ch] : m;
+      mo = p == 1 ? medo[1][ch] : mo;
+      mo = p == 2 ? medo[2][ch] : mo;
+      mo = p == 3 ? medo[3][ch] : mo;
+      pmedo[ch] = mo;
       q = p == 1 ? wi[1][ch] : q;
       q = p == 2 ? wi[2][ch] : q;
       q = p == 3 ? wi[3][ch] : q;
@@ -699,7 +728,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
       if (fast)
         return static_cast<float>(dist_int(px, wbytes, pklo, pkhi)) +
                0.25f * static_cast<float>(pnh);
-      return dist_f32<C>(S, pmed, pwi, px);
+      return dist_f32<C, false>(S, pmedo, pwi, px);
     };
     int nout = 0;
 #pragma unroll
@@ -1075,6 +1104,7 @@ template <int C>
 __global__ void __launch_bounds__(kThreads) k_composite_batch(const StackDev* __restrict__ stacks,
                                                               const int32_t* __restrict__ prefix,
                                                               int32_t n_stacks, int32_t total,
+                                                              int32_t interleave,
                                                               uint32_t* counter, uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ int item_s, stack_s;
@@ -1088,20 +1118,28 @@ __global__ void __launch_bounds__(kThreads) k_composite_batch(const StackDev* __
   for (;;) {
     if (threadIdx.x == 0) {
       const int it = static_cast<int>(atomicAdd(counter, 1u));
-      int lo = 0, hi = n_stacks;  // largest s with prefix[s] <= it
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (prefix[mid] <= it) lo = mid; else hi = mid;
+      if (interleave) {
+        // stacks of one geometry (chrono-video windows): tile-major order, so consecutive
+        // items read the same rows of mostly the same frames while they are in L2
+        stack_s = it % n_stacks;
+        item_s = it / n_stacks;
+      } else {
+        int lo = 0, hi = n_stacks;  // largest s with prefix[s] <= it
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (prefix[mid] <= it) lo = mid; else hi = mid;
+        }
+        stack_s = lo;
+        item_s = it - prefix[lo];
       }
-      item_s = it;
-      stack_s = lo;
+      if (it >= total) item_s = -1;
     }
     __syncthreads();
-    const int it = item_s, s = stack_s;
-    if (it >= total) break;
+    const int tile = item_s, s = stack_s;
+    if (tile < 0) break;
     const StackDev& S = stacks[s];
     uint32_t warn = 0;
-    if (!run_tile<C>(S, tile_geo(S, it - prefix[s]), L, phase, error, warn)) return;
+    if (!run_tile<C>(S, tile_geo(S, tile), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
   }
 }

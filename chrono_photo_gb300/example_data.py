@@ -113,7 +113,8 @@ def video_stack(seed=3, n=300, w=1920, h=1080, out=None):
 
 def shake_stack(seed=5, n=100, w=6000, h=4000, max_shift=12):
     """Textured background translated per frame by U[-12, 12]^2, 5 disks. Returns
-    (frames, shifts) with shifts[i] = translation of frame i (frame 0's is the reference)."""
+    (frames, shifts): frame i shows the background window at shifts[i], so the shake offsets
+    of frame i relative to frame 0 are shifts[0] - shifts[i]."""
     rng = np.random.default_rng(seed + 1000)
     shifts = rng.integers(-max_shift, max_shift + 1, size=(n, 2))
     frames = stack(n, w, h, sigma=3, n_disks=5, rmin=20, rmax=60, seed=seed, texture=True,

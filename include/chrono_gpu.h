@@ -207,6 +207,20 @@ int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks, const cp_para
                               int32_t n_stacks, uint8_t* const* outs,
                               uint8_t* const* out_blends, uint64_t* warnings, void* stream);
 
+/* Chrono-video over frames resident on the device: one composite per window of
+ * cp_video_windows (win_start/win_len/win_indices index into `frames`, image_count device
+ * frame pointers). Windows of length 0 are skipped (src/main.rs:326-328); outs, out_blends
+ * (nullable) and warnings (device, nullable) are indexed by window. Each window's absolute
+ * fade is evaluated at its first index (src/chrono.rs:103). One persistent launch, work
+ * ordered tile-major so that overlapping windows read shared frame rows while they are in
+ * L2. Replaces create_video's loop over create_frame, src/main.rs:254-323. */
+int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* frames, int32_t image_count,
+                              int32_t width, int32_t height, int32_t channels,
+                              int32_t n_windows, const int64_t* win_start,
+                              const int32_t* win_len, const int32_t* win_indices,
+                              const cp_params* params, uint8_t* const* outs,
+                              uint8_t* const* out_blends, uint64_t* warnings, void* stream);
+
 /* ---- camera shake -------------------------------------------------------------------- */
 /* ShakeAnalyzer::analyze (src/shake.rs:190-313): anchor windows of radius anchor_radius
  * from frame 0, exhaustive wrapping-i32 sum of squared differences over the
