@@ -47,9 +47,9 @@ def _texture(rng, w, h, k=8):
     ys = np.arange(h, dtype=np.float32)[:, None]
     t = np.zeros((h, w), np.float32)
     for _ in range(k):
-        fx, fy = rng.uniform(0.005, 0.06, size=2)
+        fx, fy = rng.uniform(0.04, 0.35, size=2)
         ph = rng.uniform(0, 2 * np.pi)
-        amp = rng.uniform(4, 12)
+        amp = rng.uniform(6, 16)
         t += amp * np.sin(fx * xs + fy * ys + ph).astype(np.float32)
     return t[..., None]
 
@@ -111,14 +111,14 @@ def video_stack(seed=3, n=300, w=1920, h=1080, out=None):
                  drift=0.05, out=out)
 
 
-def shake_stack(seed=5, n=100, w=6000, h=4000, max_shift=12):
+def shake_stack(seed=5, n=100, w=6000, h=4000, max_shift=12, n_disks=5, rmin=20, rmax=60):
     """Textured background translated per frame by U[-12, 12]^2, 5 disks. Returns
     (frames, shifts): frame i shows the background window at shifts[i], so the shake offsets
     of frame i relative to frame 0 are shifts[0] - shifts[i]."""
     rng = np.random.default_rng(seed + 1000)
     shifts = rng.integers(-max_shift, max_shift + 1, size=(n, 2))
-    frames = stack(n, w, h, sigma=3, n_disks=5, rmin=20, rmax=60, seed=seed, texture=True,
-                   shifts=shifts)
+    frames = stack(n, w, h, sigma=3, n_disks=n_disks, rmin=rmin, rmax=rmax, seed=seed,
+                   texture=True, shifts=shifts)
     return frames, shifts
 
 
