@@ -5,5 +5,5 @@ C ABI. This package builds it in-tree (build.py), binds it with ctypes (_abi.py)
 the reference's processor interface in Python (api.py).
 """
 from ._abi import ChronoError, lib  # noqa: F401
-from .api import (Context, Crop, Fade, OutlierProcessor, ShakeAnalyzer,  # noqa: F401
+from .api import (Context, Crop, Fade, OutlierProcessor, Server, ShakeAnalyzer,  # noqa: F401
                   SimpleProcessor, Threshold, default_context, make_params, video_windows)

@@ -365,3 +365,62 @@ def video_windows(image_count, video_in, video_out=(None, None, 1)):
                                         frames.ctypes.data_as(_abi.I32P)), "windows")
     return [(int(frames[k]), [int(v) for v in idx[starts[k]:starts[k] + lens[k]]])
             for k in range(nw.value)]
+
+
+class Server:
+    """Continuous-batching server (cp_server_*): submit host-memory stacks as they arrive,
+    wait for results. Frames given `keys` stay resident on the device and are shared by
+    later jobs with the same keys (overlapping chrono-video windows)."""
+
+    def __init__(self, context, hbm_budget=0, max_inflight=8):
+        self.ctx = context
+        h = ct.c_void_p()
+        context.check(lib().cp_server_create(context.handle, hbm_budget, max_inflight,
+                                             ct.byref(h)), "cp_server_create")
+        self.handle = h
+        self.pending = {}
+
+    def submit(self, frames, params=None, keys=None, blend=True, frame_offset=0, **kw):
+        keep = []
+        p = params if params is not None else make_params(keep=keep, **kw)
+        a = _as_stack(frames)
+        n, h, w, c = a.shape
+        job = _abi.Job()
+        job.stack = _abi.Stack(n=n, width=w, height=h, channels=c, base=a.ctypes.data,
+                               frame_stride=h * w * c, frame_offset=frame_offset)
+        if keys is not None:
+            karr = (ct.c_uint64 * n)(*[int(k) for k in keys])
+            keep.append(karr)
+            job.frame_keys = ct.cast(karr, ct.POINTER(ct.c_uint64))
+        job.params = p
+        out = np.empty((h, w, c), np.uint8)
+        bl = np.empty((h, w, c), np.uint8) if blend else None
+        job.out = out.ctypes.data
+        job.out_blend = bl.ctypes.data if bl is not None else None
+        jid = ct.c_uint64()
+        self.ctx.check(lib().cp_server_submit(self.handle, ct.byref(job), ct.byref(jid)),
+                       "cp_server_submit")
+        self.pending[jid.value] = (a, out, bl, keep, p)
+        return jid.value
+
+    def wait(self, job_id, timeout_ms=-1):
+        r = _abi.JobResult()
+        rc = lib().cp_server_wait(self.handle, job_id, timeout_ms, ct.byref(r))
+        if rc == _abi.CP_ERR_TIMEOUT:
+            return None
+        self.ctx.check(rc, "cp_server_wait")
+        a, out, bl, keep, p = self.pending.pop(job_id)
+        return {"status": r.status, "warnings": r.warnings, "submit_s": r.submit_s,
+                "admit_s": r.admit_s, "done_s": r.done_s, "out": out, "blend": bl}
+
+    def close(self):
+        if self.handle:
+            rc = lib().cp_server_destroy(self.handle)
+            self.handle = None
+            self.ctx.check(rc, "cp_server_destroy")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

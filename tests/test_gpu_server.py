@@ -1,0 +1,74 @@
+"""The continuous-batching server (needs a GB300): every job's result is the same alone and
+in the mix; keyed frames are shared between jobs; the HBM budget is enforced."""
+import numpy as np
+import pytest
+
+import chrono_photo_gb300 as cg
+from chrono_photo_gb300 import _abi
+from oracle import oracle
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+MODES = [dict(outlier="extreme", background="first"), dict(outlier="average", background="average"),
+         dict(outlier="first", background="median"), dict(outlier="last", background="random"),
+         dict(outlier="forward", background="first", threshold="rel/2/4")]
+
+
+def test_results_same_alone_and_in_mix(ctx):
+    rng = np.random.default_rng(0)
+    jobs = []
+    for i in range(14):
+        n = int(rng.integers(3, 70))
+        h, w = [(16, 24), (40, 64), (33, 70), (64, 64)][i % 4]
+        c = 1 if i % 5 == 4 else 3
+        frames = cases.random_stack(rng, n, h, w, c, n_spots=4)
+        kw = dict(MODES[i % len(MODES)])
+        if i % 7 == 6:
+            kw = dict(mode="lighter")
+        jobs.append((frames, kw))
+    alone = [ctx.composite(f, cases.params(**kw)) for f, kw in jobs]
+    with cg.Server(ctx, max_inflight=6) as srv:
+        ids = [srv.submit(f, cases.params(**kw)) for f, kw in jobs]
+        res = [srv.wait(j) for j in ids]
+    for (f, kw), a, r in zip(jobs, alone, res):
+        assert r["status"] == 0
+        assert np.array_equal(r["out"], a[0])
+        if kw.get("mode", "outlier") == "outlier":
+            assert np.array_equal(r["blend"], a[1])
+            assert r["warnings"] == a[2]
+        assert r["submit_s"] <= r["admit_s"] <= r["done_s"]
+
+
+def test_shared_keyed_frames(ctx):
+    """Overlapping windows submitted with frame keys: frames upload once and are shared."""
+    rng = np.random.default_rng(1)
+    pool = cases.random_stack(rng, 20, 24, 40, 3, n_spots=5)
+    wins = [list(range(s, s + 8)) for s in range(0, 13)]
+    with cg.Server(ctx) as srv:
+        ids = [srv.submit(pool[w], cases.params(outlier="forward", background="first",
+                                                fade="clamp/abs/0,0.5/12,1"),
+                          keys=[1000 + i for i in w], frame_offset=w[0]) for w in wins]
+        res = [srv.wait(j) for j in ids]
+    for w, r in zip(wins, res):
+        p = cases.params(outlier="forward", background="first", fade="clamp/abs/0,0.5/12,1")
+        ref = oracle.composite(pool[w], p, frame_offset=w[0])
+        assert r["status"] == 0
+        assert np.array_equal(r["out"], ref[0]) and np.array_equal(r["blend"], ref[1])
+
+
+def test_budget(ctx):
+    rng = np.random.default_rng(2)
+    small = cases.random_stack(rng, 4, 16, 16, 3)
+    big = cases.random_stack(rng, 40, 128, 128, 3)  # ~2 MB of frames
+    with cg.Server(ctx, hbm_budget=1 << 20) as srv:
+        a = srv.submit(small, cases.params())
+        b = srv.submit(big, cases.params())
+        ra, rb = srv.wait(a), srv.wait(b)
+    assert ra["status"] == 0 and rb["status"] == _abi.CP_ERR_BUDGET
+
+
+def test_invalid_job_rejected(ctx):
+    with cg.Server(ctx) as srv:
+        with pytest.raises(_abi.ChronoError):
+            srv.submit(np.zeros((2, 4, 4, 3), np.uint8), cases.params(threshold="rel/1/2"))
