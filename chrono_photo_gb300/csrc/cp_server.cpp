@@ -239,10 +239,14 @@ void release(cp_server* srv, Job* j) {
   }
 }
 
-bool frames_ready(const Job* j) {
-  for (const Frame* f : j->frames)
-    if (cudaEventQuery(f->ready) != cudaSuccess) return false;
-  return true;
+// 1: every frame of the job is on the device; 0: copies still in flight; -1: a copy failed.
+int frames_ready(const Job* j) {
+  for (const Frame* f : j->frames) {
+    const cudaError_t q = cudaEventQuery(f->ready);
+    if (q == cudaErrorNotReady) return 0;
+    if (q != cudaSuccess) return -1;
+  }
+  return 1;
 }
 
 // One persistent launch over the tiles of `batch` (same channel count).
@@ -367,8 +371,21 @@ void worker_loop(cp_server* srv) {
     }
     // 2. launch every admitted job whose frames have landed, one launch per channel count
     std::map<int, std::vector<Job*>> ready;
-    for (Job* j : srv->active)
-      if (j->state == 1 && frames_ready(j)) ready[j->spec.stack.channels].push_back(j);
+    for (Job* j : srv->active) {
+      if (j->state != 1) continue;
+      const int fr = frames_ready(j);
+      if (fr > 0) {
+        ready[j->spec.stack.channels].push_back(j);
+      } else if (fr < 0) {
+        cudaGetLastError();
+        release(srv, j);
+        j->res.status = CP_ERR_CUDA;
+        j->res.done_s = now_s();
+        j->state = 3;
+        srv->cv_done.notify_all();
+        progressed = true;
+      }
+    }
     for (auto& kv : ready) {
       std::vector<Job*>& b = kv.second;
       for (size_t i = 0; i < b.size(); i += kMaxBatch) {
@@ -391,7 +408,19 @@ void worker_loop(cp_server* srv) {
     // 3. completions
     for (auto it = srv->active.begin(); it != srv->active.end();) {
       Job* j = *it;
-      if (j->state == 2 && cudaEventQuery(j->done_ev) == cudaSuccess) {
+      const cudaError_t q = j->state == 2 ? cudaEventQuery(j->done_ev) : cudaErrorNotReady;
+      if (j->state == 2 && q != cudaSuccess && q != cudaErrorNotReady) {  // the launch failed
+        cudaGetLastError();
+        cudaEventDestroy(j->done_ev);
+        j->done_ev = nullptr;
+        release(srv, j);
+        j->res.status = CP_ERR_CUDA;
+        j->res.done_s = now_s();
+        j->state = 3;
+        it = srv->active.erase(it);
+        srv->cv_done.notify_all();
+        progressed = true;
+      } else if (j->state == 2 && q == cudaSuccess) {
         cudaEventDestroy(j->done_ev);
         j->done_ev = nullptr;
         const cp_stack& st = j->spec.stack;
