@@ -18,6 +18,7 @@ CP_ERR_BUDGET = -5
 CP_ERR_RANGE = -6
 CP_ERR_STATE = -7
 CP_ERR_NODEV = -8
+CP_ERR_LIMIT = -9
 
 MODE = {"outlier": 0, "darker": 1, "lighter": 2}
 OUTLIER = {"first": 0, "last": 1, "extreme": 2, "average": 3, "forward": 4, "backward": 5}
@@ -100,6 +101,8 @@ SIGNATURES = [
     ("cp_composite_video_device", ct.c_int, [P, ct.POINTER(P), I32, I32, I32, I32, I32, I64P,
                                              I32P, I32P, ct.POINTER(Params), ct.POINTER(P),
                                              ct.POINTER(P), P, P]),
+    ("cp_composite_batch_static", ct.c_int, [ct.POINTER(Stack), ct.POINTER(Params), I32,
+                                             ct.POINTER(P), ct.POINTER(P), P, P]),
     ("cp_shake_analyze_device", ct.c_int, [P, ct.POINTER(P), I32, I32, I32, I32, I32P, I32,
                                            I32, I32, I32P, I32P]),
     ("cp_server_create", ct.c_int, [P, U64, I32, ct.POINTER(P)]),
@@ -121,7 +124,8 @@ class ChronoError(RuntimeError):
 STATUS_NAMES = {CP_OK: "ok", CP_ERR_ARG: "invalid argument", CP_ERR_OOM: "out of memory",
                 CP_ERR_TIMEOUT: "timed out", CP_ERR_CUDA: "CUDA error",
                 CP_ERR_BUDGET: "HBM budget exceeded", CP_ERR_RANGE: "out of range",
-                CP_ERR_STATE: "invalid state", CP_ERR_NODEV: "no sm_103 device"}
+                CP_ERR_STATE: "invalid state", CP_ERR_NODEV: "no sm_103 device",
+                CP_ERR_LIMIT: "above a fixed limit"}
 
 
 def lib():

@@ -429,6 +429,7 @@ const char* cp_status_str(int status) {
     case CP_ERR_RANGE: return "coordinate out of range";
     case CP_ERR_STATE: return "invalid state";
     case CP_ERR_NODEV: return "no sm_103 device";
+    case CP_ERR_LIMIT: return "request above the fixed limit of the allocation-free entry point";
     default: return "unknown status";
   }
 }

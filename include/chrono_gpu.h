@@ -43,6 +43,7 @@ extern "C" {
 #define CP_ERR_RANGE (-6)   /* shake window outside the image (reference: panic, shake.rs:336) */
 #define CP_ERR_STATE (-7)   /* object in the wrong state (stopped server, unknown job)     */
 #define CP_ERR_NODEV (-8)   /* no CUDA device with compute capability 10.3                 */
+#define CP_ERR_LIMIT (-9)   /* request above a fixed limit of cp_composite_batch_static    */
 
 /* ---- option enums (src/options.rs) --------------------------------------------------- */
 /* SelectionMode, src/options.rs:8-31 */
@@ -220,6 +221,23 @@ int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* frames, int32_t
                               const int32_t* win_len, const int32_t* win_indices,
                               const cp_params* params, uint8_t* const* outs,
                               uint8_t* const* out_blends, uint64_t* warnings, void* stream);
+
+/* Allocation-free form of cp_composite_batch_device, for callers that cannot call
+ * cudaMalloc (code running while a CUDA graph is captured, plug-ins whose host owns all
+ * device memory, services with a fixed footprint). No counterpart in the reference. It needs
+ * no context: it runs on the current device and stream `stream`, and keeps its scratch
+ * (stack descriptors, tile prefix sums, work counter) in one fixed __device__ array of
+ * about 190 KB that every GPU loading the library holds until exit. At most
+ * CP_STATIC_MAX_STACKS stacks per call (more: CP_ERR_LIMIT). The first call on a device
+ * looks up the array's device address; make that first call before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU (other streams, other host
+ * threads) race: order them on one stream. Inputs, outputs and warnings (device array of
+ * n_stacks counters, nullable) are as for cp_composite_batch_device; the launch is not
+ * graph-cached. Asynchronous. */
+#define CP_STATIC_MAX_STACKS 64
+int cp_composite_batch_static(const cp_stack* stacks, const cp_params* params, int32_t n_stacks,
+                              uint8_t* const* outs, uint8_t* const* out_blends,
+                              uint64_t* warnings, void* stream);
 
 /* ---- camera shake -------------------------------------------------------------------- */
 /* ShakeAnalyzer::analyze (src/shake.rs:190-313): anchor windows of radius anchor_radius

@@ -1,0 +1,84 @@
+"""The allocation-free batched entry point, cp_composite_batch_static (needs a GB300).
+
+It exists for callers that cannot call cudaMalloc (graph capture in progress, a host
+application that owns all device memory, a fixed footprint): its scratch is a fixed device
+array inside the library. Its output must equal cp_composite_batch_device's on the same
+inputs, on two calls in a row (the second call finds the previous call's scratch contents).
+The test allocates its own inputs and outputs; the entry point allocates nothing."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+import chrono_photo_gb300 as cg
+from chrono_photo_gb300 import _abi
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def test_static_batch_equals_batch_device(ctx):
+    rng = np.random.default_rng(7)
+    specs = [(9, 20, 33, dict(mode="outlier", outlier="extreme", background="first")),
+             (40, 48, 64, dict(mode="outlier", outlier="forward", background="average",
+                               fade="clamp/abs/0,0.2/30,1")),
+             (70, 17, 300, dict(mode="outlier", threshold="rel/2/5", outlier="average",
+                                background="median")),
+             (25, 31, 41, dict(mode="darker"))]
+    n_st = len(specs)
+    ptrs = []
+    keep = []
+    try:
+        stacks = (_abi.Stack * n_st)()
+        params = (_abi.Params * n_st)()
+        outs = {k: (ct.c_void_p * n_st)() for k in ("dev", "st")}
+        blends = {k: (ct.c_void_p * n_st)() for k in ("dev", "st")}
+        shapes = []
+        for i, (n, h, w, kw) in enumerate(specs):
+            frames = cases.random_stack(rng, n, h, w, 3, n_spots=5)
+            base = ctx.upload(frames)
+            ptrs.append(base)
+            stacks[i] = _abi.Stack(n=n, width=w, height=h, channels=3, base=base,
+                                   frame_stride=h * w * 3, frame_offset=i)
+            params[i] = cg.make_params(keep=keep, **kw)
+            for k in ("dev", "st"):
+                outs[k][i] = ctx.alloc(h * w * 3)
+                blends[k][i] = ctx.alloc(h * w * 3)
+                ptrs += [outs[k][i], blends[k][i]]
+            shapes.append((h, w, 3))
+        warn = {k: ctx.alloc(8 * n_st) for k in ("dev", "st")}
+        ptrs += list(warn.values())
+        stream = _abi.lib().cp_ctx_stream(ctx.handle)
+        ctx.upload(np.zeros(n_st, np.uint64), warn["dev"])
+        ctx.check(_abi.lib().cp_composite_batch_device(ctx.handle, stacks, params, n_st,
+                                                       outs["dev"], blends["dev"], warn["dev"],
+                                                       stream))
+        ctx.synchronize()
+        ref = [(ctx.download(outs["dev"][i], s), ctx.download(blends["dev"][i], s))
+               for i, s in enumerate(shapes)]
+        ref_warn = ctx.download(warn["dev"], (n_st,), np.uint64)
+        for call in range(2):
+            ctx.upload(np.zeros(n_st, np.uint64), warn["st"])
+            for i, s in enumerate(shapes):  # stale outputs must be overwritten
+                ctx.upload(np.full(s, 77, np.uint8), outs["st"][i])
+            rc = _abi.lib().cp_composite_batch_static(stacks, params, n_st, outs["st"],
+                                                      blends["st"], warn["st"], stream)
+            assert rc == _abi.CP_OK, "call %d: %d" % (call, rc)
+            ctx.synchronize()
+            for i, s in enumerate(shapes):
+                cases.assert_close_u8(ctx.download(outs["st"][i], s), ref[i][0],
+                                      what="call %d composite %d" % (call, i))
+                if specs[i][3]["mode"] == "outlier":
+                    cases.assert_close_u8(ctx.download(blends["st"][i], s), ref[i][1],
+                                          what="call %d blend %d" % (call, i))
+            assert np.array_equal(ctx.download(warn["st"], (n_st,), np.uint64), ref_warn)
+    finally:
+        for p in ptrs:
+            ctx.free(p)
+
+
+def test_static_batch_limit(ctx):
+    st = (_abi.Stack * 65)()
+    pa = (_abi.Params * 65)()
+    outs = (ct.c_void_p * 65)()
+    assert _abi.lib().cp_composite_batch_static(st, pa, 65, outs, None, None, None) == _abi.CP_ERR_LIMIT
