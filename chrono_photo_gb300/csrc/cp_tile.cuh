@@ -321,18 +321,27 @@ DEVI void build_planes(uint32_t (&P)[BP][8][NW], const Rows<C, SH>& rd, int w, i
   }
 }
 
-// k-th smallest of the frames in S for BP byte positions at once (independent chains the
-// scheduler interleaves): radix select over the 8 bit planes. On return c holds the frames
-// equal to the result and kk the rank of the k-th among them.
+// Order statistics d[k] (lo) and, when `pair`, d[k+1] (hi), for BP positions at once
+// (independent chains the scheduler interleaves). One radix pass over the 8 bit planes finds
+// d[k]. Rank k+1 follows the same branches until the one step where the zero-count equals
+// rank k's remaining rank + 1: there k goes to the zero branch and k+1 to the one branch,
+// whose minimum is d[k+1]. Without such a step both end in the same run: d[k+1] = d[k].
 template <int NW, int BP>
-DEVI void radix_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], const int (&k)[BP],
-                      uint32_t (&res)[BP], uint32_t (&c)[BP][NW], int (&kk)[BP]) {
+DEVI void select_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], int k,
+                       bool pair, uint32_t (&lo)[BP], uint32_t (&hi)[BP]) {
+  uint32_t c[BP][NW], sib[BP][NW];
+  int kk[BP];
+  bool split[BP];
 #pragma unroll
   for (int j = 0; j < BP; ++j) {
 #pragma unroll
-    for (int w = 0; w < NW; ++w) c[j][w] = S[w];
-    kk[j] = k[j];
-    res[j] = 0u;
+    for (int w = 0; w < NW; ++w) {
+      c[j][w] = S[w];
+      sib[j][w] = 0u;
+    }
+    kk[j] = k;
+    lo[j] = 0u;
+    split[j] = false;
   }
 #pragma unroll
   for (int b = 7; b >= 0; --b) {
@@ -346,42 +355,46 @@ DEVI void radix_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], c
         cz += __popc(z[w]);
       }
       const bool one = kk[j] >= cz;
-      kk[j] -= one ? cz : 0;
+      const bool sp = !split[j] && cz == kk[j] + 1;  // k -> 0 branch, k+1 -> 1 branch
 #pragma unroll
-      for (int w = 0; w < NW; ++w) c[j][w] = one ? (c[j][w] ^ z[w]) : z[w];  // c & P or c & ~P
-      res[j] = (res[j] << 1) | static_cast<uint32_t>(one);
+      for (int w = 0; w < NW; ++w) {
+        const uint32_t o = c[j][w] ^ z[w];  // c & P
+        sib[j][w] = sp ? o : sib[j][w];
+        c[j][w] = one ? o : z[w];
+      }
+      split[j] = split[j] || sp;
+      kk[j] -= one ? cz : 0;
+      lo[j] = (lo[j] << 1) | static_cast<uint32_t>(one);
     }
   }
-}
-
-// Order statistics d[k] (lo) and, when `pair`, d[k+1] (hi). d[k+1] equals d[k] while the run
-// of equal values continues past rank k; otherwise it is found by a second pass.
-template <int NW, int BP>
-DEVI void select_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], int k,
-                       bool pair, uint32_t (&lo)[BP], uint32_t (&hi)[BP]) {
-  uint32_t c[BP][NW];
-  int kk[BP], kv[BP];
-#pragma unroll
-  for (int j = 0; j < BP; ++j) kv[j] = k;
-  radix_multi<NW, BP>(P, S, kv, lo, c, kk);
   bool any = false;
-  bool need[BP];
 #pragma unroll
   for (int j = 0; j < BP; ++j) {
     hi[j] = lo[j];
-    int ceq = 0;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) ceq += __popc(c[j][w]);
-    need[j] = pair && kk[j] + 1 >= ceq;
-    any |= need[j];
+    split[j] = split[j] && pair;
+    any |= split[j];
   }
   if (!__any_sync(0xffffffffu, any)) return;
-  uint32_t r2[BP];
+  uint32_t m[BP];  // minimum of the sibling set: take the 0 branch whenever it is non-empty
 #pragma unroll
-  for (int j = 0; j < BP; ++j) kv[j] = k + 1;
-  radix_multi<NW, BP>(P, S, kv, r2, c, kk);
+  for (int j = 0; j < BP; ++j) m[j] = 0u;
 #pragma unroll
-  for (int j = 0; j < BP; ++j) hi[j] = need[j] ? r2[j] : lo[j];
+  for (int b = 7; b >= 0; --b)
+#pragma unroll
+    for (int j = 0; j < BP; ++j) {
+      uint32_t z[NW];
+      uint32_t nz = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        z[w] = sib[j][w] & ~P[j][b][w];
+        nz |= z[w];
+      }
+#pragma unroll
+      for (int w = 0; w < NW; ++w) sib[j][w] = nz ? z[w] : sib[j][w];
+      m[j] = (m[j] << 1) | (nz ? 0u : 1u);
+    }
+#pragma unroll
+  for (int j = 0; j < BP; ++j) hi[j] = split[j] ? m[j] : lo[j];
 }
 
 // quantile() of src/chrono.rs:567-579 from its order statistics: (1-frac)*d[p1] +
@@ -723,8 +736,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
       pmed[ch] = m;
       pwi[ch] = q;
     }
-    auto dsq_of = [&](int f) -> float {  // dist_sq of frame f, recomputed
-      const uint32_t px = load_pixel<C, SH>(rd, f, p);
+    auto dsq_px = [&](uint32_t px) -> float {  // dist_sq of a sample, recomputed
       if (fast)
         return static_cast<float>(dist_int(px, wbytes, pklo, pkhi)) +
                0.25f * static_cast<float>(pnh);
@@ -822,39 +834,61 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
       for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(pmed[ch])) << (8 * ch);
     }
 
-    // outlier pick and blend, src/chrono.rs:377-493
+    // outlier pick and blend, src/chrono.rs:377-493. One outlier (any mode) and first / last /
+    // extreme pick a single sample: one branch-free path for every lane, where no outlier
+    // gives blend 0 (the background unchanged, mask 0). Average / forward / backward with
+    // several outliers loop over them.
     float blend = 0.0f;
     int chosen = -1;
     uint32_t mask = 0;
-    if (nout == 1) {
-      const int si = first_set<NW>(pb);
-      blend = __fmul_rn(S.fade[si], blend_value(S, __fsqrt_rn(dsq_of(si))));
-      pix = blend_into_u8<C>(pix, load_pixel<C, SH>(rd, si, p), blend);
+    const bool multi = nout > 1 && (S.outlier == CP_OUTLIER_AVERAGE ||
+                                    S.outlier == CP_OUTLIER_FORWARD ||
+                                    S.outlier == CP_OUTLIER_BACKWARD);
+    if (!multi) {
+      int si;
+      float dsq;
+      if (S.outlier == CP_OUTLIER_EXTREME) {
+        si = pick4(imax, p);
+        if (fast) {
+          const int32_t dm = pick4(dmax_i, p);
+          dsq = dm < 0 ? 0.0f : static_cast<float>(dm) + 0.25f * static_cast<float>(pnh);
+        } else {
+          dsq = pick4(dmax_f, p);
+        }
+      } else {
+        si = S.outlier == CP_OUTLIER_LAST ? last_set<NW>(pb) : first_set<NW>(pb);
+        si = si < 0 ? 0 : si;
+      }
+      const uint32_t sample = load_pixel<C, SH>(rd, si, p);
+      if (S.outlier != CP_OUTLIER_EXTREME) dsq = dsq_px(sample);
+      blend = nout == 0 ? 0.0f : __fmul_rn(S.fade[si], blend_value(S, __fsqrt_rn(dsq)));
+      pix = blend_into_u8<C>(pix, sample, blend);
       mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
-      chosen = si;
-    } else if (nout > 1) {
+      chosen = nout == 0 ? -1 : si;
+    } else {
       if (S.outlier == CP_OUTLIER_FORWARD || S.outlier == CP_OUTLIER_BACKWARD) {
         float pf[C];
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((pix >> (8 * ch)) & 0xFFu);
         float binv = 1.0f;
         auto blend_one = [&](int f) {
-          const float b = __fmul_rn(S.fade[f], blend_value(S, __fsqrt_rn(dsq_of(f))));
-          const uint32_t s = load_pixel<C, SH>(rd, f, p);
+          const uint32_t sv = load_pixel<C, SH>(rd, f, p);
+          const float bk = __fmul_rn(S.fade[f], blend_value(S, __fsqrt_rn(dsq_px(sv))));
           // blend_into_f32_u8, src/color.rs:32-44
-          if (b <= 0.0f) {
-          } else if (b >= 1.0f) {
+          if (bk <= 0.0f) {
+          } else if (bk >= 1.0f) {
 #pragma unroll
-            for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((s >> (8 * ch)) & 0xFFu);
+            for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((sv >> (8 * ch)) & 0xFFu);
           } else {
 #pragma unroll
             for (int ch = 0; ch < C; ++ch) {
-              const float sv = static_cast<float>((s >> (8 * ch)) & 0xFFu);
-              pf[ch] = __fadd_rn(pf[ch], __fmul_rn(__fsub_rn(sv, pf[ch]), b));
+              const float x = static_cast<float>((sv >> (8 * ch)) & 0xFFu);
+              pf[ch] = __fadd_rn(pf[ch], __fmul_rn(__fsub_rn(x, pf[ch]), bk));
             }
           }
-          binv = __fmul_rn(binv, __fsub_rn(1.0f, b));
+          binv = __fmul_rn(binv, __fsub_rn(1.0f, bk));
         };
+        // outliers in ascending (forward) or descending (backward) frame order
         if (S.outlier == CP_OUTLIER_FORWARD) {
 #pragma unroll
           for (int w = 0; w < NW; ++w) {
@@ -881,11 +915,11 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
         for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(pf[ch])) << (8 * ch);
         mask = sat_u8(rround(__fmul_rn(__fsub_rn(1.0f, binv), 255.0f)));
         chosen = -2;
-      } else {
+      } else {  // average, src/chrono.rs:429-468
         int si;
         float dist;
         uint32_t sample;
-        if (S.outlier == CP_OUTLIER_AVERAGE) {
+        {
           uint32_t osum[C];
 #pragma unroll
           for (int ch = 0; ch < C; ++ch) osum[ch] = 0u;
@@ -899,7 +933,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
               const uint32_t px = load_pixel<C, SH>(rd, f, p);
 #pragma unroll
               for (int ch = 0; ch < C; ++ch) osum[ch] += (px >> (8 * ch)) & 0xFFu;
-              mdist = __fadd_rn(mdist, __fsqrt_rn(dsq_of(f)));
+              mdist = __fadd_rn(mdist, __fsqrt_rn(dsq_px(px)));
             }
           }
           const float kf = static_cast<float>(nout);
@@ -909,26 +943,6 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
             sample |= sat_u8(rround(__fdiv_rn(static_cast<float>(osum[ch]), kf))) << (8 * ch);
           si = 0;  // src/chrono.rs:467: the fade of an averaged outlier is taken at frame 0
           dist = __fdiv_rn(mdist, kf);
-        } else {
-          float dsq;
-          if (S.outlier == CP_OUTLIER_FIRST) {
-            si = first_set<NW>(pb);
-            dsq = dsq_of(si);
-          } else if (S.outlier == CP_OUTLIER_LAST) {
-            si = last_set<NW>(pb);
-            dsq = dsq_of(si);
-          } else {  // extreme
-            si = pick4(imax, p);
-            if (fast) {
-              const int32_t dm = pick4(dmax_i, p);
-              dsq = dm < 0 ? 0.0f
-                           : static_cast<float>(dm) + 0.25f * static_cast<float>(pnh);
-            } else {
-              dsq = pick4(dmax_f, p);
-            }
-          }
-          sample = load_pixel<C, SH>(rd, si, p);
-          dist = __fsqrt_rn(dsq);
         }
         blend = __fmul_rn(S.fade[si], blend_value(S, dist));
         pix = blend_into_u8<C>(pix, sample, blend);
