@@ -36,12 +36,12 @@ static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_
   StackDev* d_stacks = static_cast<StackDev*>(plan.dev);
   int32_t* d_prefix = reinterpret_cast<int32_t*>(d_stacks + n_stacks);
   uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + n_stacks + 1);
-  const int smem = smem_bytes_for(max_n, kTilePx, channels);
+  const int smem = smem_bytes_for(max_n, channels);
   int per_sm = 1;
   switch (channels) {
-    case 1: per_sm = composite_max_ctas_c1(kThreads, smem); break;
-    case 3: per_sm = composite_max_ctas_c3(kThreads, smem); break;
-    default: per_sm = composite_max_ctas_c4(kThreads, smem); break;
+    case 1: per_sm = composite_max_ctas_c1(cta_threads(1), smem); break;
+    case 3: per_sm = composite_max_ctas_c3(cta_threads(3), smem); break;
+    default: per_sm = composite_max_ctas_c4(cta_threads(4), smem); break;
   }
   const int grid = std::max(1, std::min(plan.total, per_sm * ctx->sm_count));
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), st);
@@ -89,7 +89,7 @@ static int batch_run(cp_ctx* ctx, const cp_stack* stacks, const cp_params* param
     max_n = std::max(max_n, s.n);
     prefix[static_cast<size_t>(i) + 1] = prefix[static_cast<size_t>(i)] + d.tiles;
   }
-  if (smem_bytes_for(max_n, kTilePx, channels) > ctx->max_smem) return CP_ERR_ARG;
+  if (smem_bytes_for(max_n, channels) > ctx->max_smem) return CP_ERR_ARG;
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
 
   // find a plan with the same descriptors

@@ -148,9 +148,9 @@ int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
     if (reinterpret_cast<uintptr_t>(dev_frames[i]) & 15) shifted = true;
   }
   d->shifted = shifted;
-  d->threads = kThreads;
+  d->threads = cta_threads(st->channels);
   d->tile_px = kTilePx;
-  d->nw = n <= 32 ? 1 : (n <= 64 ? 2 : 4);
+  d->nw = nw_for(n);
   d->px_begin = 0;
   d->px_end = st->width * st->height;
   d->row_begin = 0;
@@ -281,7 +281,7 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
     }
     return cuda_status(ctx, static_cast<cudaError_t>(rc), "simple launch");
   }
-  const int smem = smem_bytes_for(d.n, d.tile_px, d.channels);
+  const int smem = smem_bytes_for(d.n, d.channels);
   if (smem > ctx->max_smem) {
     ctx_error(ctx, "tile needs %d bytes of shared memory", smem);
     return CP_ERR_ARG;

@@ -6,9 +6,37 @@
 
 namespace cp {
 
-constexpr int kPixPerThread = 4;   // a thread owns 4 pixels = `channels` words per frame row
-constexpr int kThreads = 64;       // CTA size of the compositing kernels
-constexpr int kTilePx = kPixPerThread * kThreads;
+constexpr int kPixPerThread = 4;  // a column is 4 pixels = `channels` words per frame row
+constexpr int kTilePx = 128;      // pixels per tile: 32 columns, served by `channels` warps
+inline int cta_threads(int channels) { return 32 * channels; }
+
+// Shared-memory exchange area of a compositing tile, behind its staged frame rows: warp w
+// builds the order statistics of word w of every column, every warp the distance pass over
+// its frame class, the epilogue is split by pixel; results cross warps here.
+// The column index is innermost everywhere, so a warp's accesses hit 32 distinct banks.
+template <int C, int NW>
+struct Aux {
+  uint32_t lo[C][32], hi[C][32];  // word w of column t: order statistics d[k], d[k+1]
+  float wi[C][4][32];             // rel threshold: w * iqr_inv per position of word w
+  uint32_t bits[C][4][NW][32];    // per frame class, pixel, flag word, column
+  int32_t best[C][4][32];         // integer path: max (D' << 8) + 255 - f; f32 path: max distance
+  int32_t imf[C][4][32];          // f32 path: frame of that maximum
+  uint32_t out[C][32], blend[C][32];  // the tile's output rows, C words per column
+};
+inline int aux_bytes(int channels, int nw) {
+  switch (channels * 8 + nw) {
+    case 8 + 1: return sizeof(Aux<1, 1>);
+    case 8 + 2: return sizeof(Aux<1, 2>);
+    case 8 + 4: return sizeof(Aux<1, 4>);
+    case 24 + 1: return sizeof(Aux<3, 1>);
+    case 24 + 2: return sizeof(Aux<3, 2>);
+    case 24 + 4: return sizeof(Aux<3, 4>);
+    case 32 + 1: return sizeof(Aux<4, 1>);
+    case 32 + 2: return sizeof(Aux<4, 2>);
+    default: return sizeof(Aux<4, 4>);
+  }
+}
+inline int nw_for(int n) { return n <= 32 ? 1 : (n <= 64 ? 2 : 4); }
 
 // Device-side descriptor of one stack and its options, prepared on the host from cp_stack
 // and cp_params. A single-stack launch passes it by value (kernel parameter space, so the
@@ -64,9 +92,13 @@ struct StackDev {
   float fade[CP_MAX_FRAMES];  // fade(i, n, frame_offset)
 };
 
-inline int row_pitch_host(int tile_px, int channels) { return tile_px * channels + 32; }
-inline int smem_bytes_for(int n, int tile_px, int channels) {
-  return 256 + n * row_pitch_host(tile_px, channels);
+inline int row_pitch_host(int channels) { return kTilePx * channels + 32; }
+// Shared-memory header of a compositing CTA: mbarrier, per-row byte shifts, and the cached
+// frame base pointers of the stack being processed.
+constexpr int kSmemHeader = 256 + 8 * CP_MAX_FRAMES;
+// header + n staged rows + the exchange area
+inline int smem_bytes_for(int n, int channels) {
+  return kSmemHeader + n * row_pitch_host(channels) + aux_bytes(channels, nw_for(n));
 }
 
 // Per-channel-count kernel entry points (cp_kernels_c*.cu). Return cudaError_t values.

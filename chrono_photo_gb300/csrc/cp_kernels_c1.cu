@@ -24,7 +24,7 @@ int launch_batch_c1(const StackDev* stacks, const int32_t* prefix, int32_t n_sta
                      int grid, int smem, void* stream) {
   cudaFuncSetAttribute(reinterpret_cast<const void*>(&k_composite_batch<1>),
                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_composite_batch<1><<<grid, 64, smem, static_cast<cudaStream_t>(stream)>>>(
+  k_composite_batch<1><<<grid, 32 * 1, smem, static_cast<cudaStream_t>(stream)>>>(
       stacks, prefix, n_stacks, total, interleave, counter, error);
   return static_cast<int>(cudaGetLastError());
 }

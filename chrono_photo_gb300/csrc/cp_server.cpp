@@ -303,12 +303,12 @@ int launch_jobs(cp_server* srv, std::vector<Job*>& batch) {
                   cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), st);
   const int channels = batch[0]->spec.stack.channels;
-  const int smem = smem_bytes_for(max_n, kTilePx, channels);
+  const int smem = smem_bytes_for(max_n, channels);
   int per_sm = 1;
   switch (channels) {
-    case 1: per_sm = composite_max_ctas_c1(kThreads, smem); break;
-    case 3: per_sm = composite_max_ctas_c3(kThreads, smem); break;
-    default: per_sm = composite_max_ctas_c4(kThreads, smem); break;
+    case 1: per_sm = composite_max_ctas_c1(cta_threads(1), smem); break;
+    case 3: per_sm = composite_max_ctas_c3(cta_threads(3), smem); break;
+    default: per_sm = composite_max_ctas_c4(cta_threads(4), smem); break;
   }
   const int grid = std::max(1, std::min(prefix.back(), per_sm * ctx->sm_count));
   int rc = 0;

@@ -95,7 +95,7 @@ extern "C" int cp_composite_batch_static(const cp_stack* stacks, const cp_params
                                           cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return CP_ERR_CUDA;
   }
-  const int smem = smem_bytes_for(max_n, kTilePx, channels);
+  const int smem = smem_bytes_for(max_n, channels);
   if (smem > max_smem) return CP_ERR_ARG;
   uint32_t* counter = reinterpret_cast<uint32_t*>(scratch + kCounterOffset);
   uint32_t* error = counter + 1;
@@ -106,9 +106,9 @@ extern "C" int cp_composite_batch_static(const cp_stack* stacks, const cp_params
   if (e != cudaSuccess) return CP_ERR_CUDA;
   int per_sm = 1;
   switch (channels) {
-    case 1: per_sm = composite_max_ctas_c1(kThreads, smem); break;
-    case 3: per_sm = composite_max_ctas_c3(kThreads, smem); break;
-    case 4: per_sm = composite_max_ctas_c4(kThreads, smem); break;
+    case 1: per_sm = composite_max_ctas_c1(cta_threads(1), smem); break;
+    case 3: per_sm = composite_max_ctas_c3(cta_threads(3), smem); break;
+    case 4: per_sm = composite_max_ctas_c4(cta_threads(4), smem); break;
     default: return CP_ERR_ARG;
   }
   const int grid = prefix[n_stacks] < per_sm * sms ? prefix[n_stacks] : per_sm * sms;

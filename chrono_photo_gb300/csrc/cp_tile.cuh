@@ -35,7 +35,6 @@ namespace {
 
 #define DEVI __device__ __forceinline__
 
-constexpr int kSmemHeader = 256;            // mbarrier + per-frame byte shifts
 constexpr long long kWaitCycles = 1ll << 32; // ~2 s at 2 GHz before a wait gives up
 #ifndef CP_DUNROLL
 #define CP_DUNROLL 2
@@ -143,15 +142,25 @@ DEVI TileGeo tile_geo(const StackDev& S, int t) {
 template <int C>
 constexpr int kPitch = kTilePx * C + 32;
 
-// Warp 0 stages the n frame rows of a tile into `buf` (row f at f * pitch). A source that is
-// not 16-byte aligned (cropped stacks, unaligned frames) is copied from the aligned address
-// below it and the offset is recorded in shifts[f]. Must be called by all 32 lanes of warp 0.
+// Warp 0 stages the n frame rows of a tile into `buf` (row f at f * pitch) from the frame
+// bases cached in shared memory. A source that is not 16-byte aligned (cropped stacks,
+// unaligned frames) is copied from the aligned address below it and the offset is recorded
+// in shifts[f]. Must be called by all 32 lanes of warp 0.
 template <int C>
 DEVI void issue_tile(const StackDev& S, const TileGeo& g, uint8_t* buf, uint8_t* shifts,
-                     uint64_t* bar) {
+                     const uintptr_t* fbase, uint64_t* bar) {
   constexpr int pitch = kPitch<C>;
   const int lane = threadIdx.x & 31;
-  const int row_bytes = g.npx * C;
+  const uint32_t row_bytes = static_cast<uint32_t>(g.npx * C);
+  if (!S.shifted) {  // every row starts 16-byte aligned: one size for all
+    const uint32_t sz = (row_bytes + 15u) & ~15u;
+    const uintptr_t off = static_cast<uintptr_t>(g.out_px0) * C;
+    if (lane == 0) mbar_expect_tx(bar, sz * static_cast<uint32_t>(S.n));
+    __syncwarp();
+    for (int f = lane; f < S.n; f += 32)
+      bulk_g2s(buf + (size_t)f * pitch, reinterpret_cast<const void*>(fbase[f] + off), sz, bar);
+    return;
+  }
   uint32_t total = 0;
   for (int f = lane; f < S.n; f += 32) {
     long long off;
@@ -161,7 +170,7 @@ DEVI void issue_tile(const StackDev& S, const TileGeo& g, uint8_t* buf, uint8_t*
     } else {
       off = (long long)g.out_px0 * C;
     }
-    const uintptr_t src = reinterpret_cast<uintptr_t>(S.frames[f]) + off;
+    const uintptr_t src = fbase[f] + off;
     const uintptr_t a0 = src & ~uintptr_t(15);
     const uintptr_t a1 = (src + row_bytes + 15) & ~uintptr_t(15);
     total += static_cast<uint32_t>(a1 - a0);
@@ -179,14 +188,13 @@ DEVI void issue_tile(const StackDev& S, const TileGeo& g, uint8_t* buf, uint8_t*
     } else {
       off = (long long)g.out_px0 * C;
     }
-    const uintptr_t src = reinterpret_cast<uintptr_t>(S.frames[f]) + off;
+    const uintptr_t src = fbase[f] + off;
     const uintptr_t a0 = src & ~uintptr_t(15);
     const uintptr_t a1 = (src + row_bytes + 15) & ~uintptr_t(15);
     bulk_g2s(buf + (size_t)f * pitch, reinterpret_cast<const void*>(a0),
              static_cast<uint32_t>(a1 - a0), bar);
   }
 }
-
 
 // ---- shared-memory rows ------------------------------------------------------------------------
 // Word w (0..C-1) of this thread's 4-pixel column in frame row f. SHIFTED rows start
@@ -465,277 +473,278 @@ DEVI int last_set(const uint32_t (&b)[NW]) {
 }
 
 
-// Store the 4 pixel words of a thread (C bytes each) to out at the tile's position: C
-// aligned 32-bit stores for a full, aligned group, else byte stores of the valid pixels.
+// ---- tile exchange area ------------------------------------------------------------------
+// A tile is 32 columns x 4 pixels, served by C warps: warp w builds the planes and order
+// statistics of word w of every column, all warps run the distance pass over the frames of
+// their residue class (f = w mod C), and the epilogue is split by pixel. Results move between
+// warps through this shared-memory area behind the staged rows.
+
+// Per-pixel statistics of column t from the words' order statistics (positions q = p*C + ch).
 template <int C>
-DEVI void store_pixels(uint8_t* out, const TileGeo& g, int tid, const uint32_t (&pw)[4]) {
-  const int first = 4 * tid;
-  if (first >= g.npx) return;
-  uint8_t* dst = out + static_cast<size_t>(g.out_px0 + first) * C;
-  if (first + 4 <= g.npx && (reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
-    uint32_t ow[C];
+struct PixStats {
+  uint32_t klo, khi;  // floor / ceil of the medians, channel bytes (integer path)
+  int nh;             // channels with a half-integer median
+  float med[C], medo[C], wi[C];
+};
+template <int C, int NW>
+DEVI PixStats<C> pixel_stats(const StackDev& S, const Aux<C, NW>& A, int t, int p) {
+  PixStats<C> r;
+  r.klo = r.khi = 0u;
+  r.nh = 0;
+  const bool rel = !S.thr_abs;
 #pragma unroll
-    for (int i = 0; i < C; ++i) ow[i] = 0u;
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) {
-        const int q = p * C + ch;
-        ow[q / 4] |= ((pw[p] >> (8 * ch)) & 0xFFu) << (8 * (q % 4));
-      }
-    uint32_t* o32 = reinterpret_cast<uint32_t*>(dst);
-#pragma unroll
-    for (int i = 0; i < C; ++i) o32[i] = ow[i];
-  } else {
-#pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      if (first + p >= g.npx) break;
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) dst[p * C + ch] = static_cast<uint8_t>(pw[p] >> (8 * ch));
+  for (int ch = 0; ch < C; ++ch) {
+    const int q = p * C + ch;
+    const uint32_t lo = (A.lo[q >> 2][t] >> (8 * (q & 3))) & 0xFFu;
+    const uint32_t hi = (A.hi[q >> 2][t] >> (8 * (q & 3))) & 0xFFu;
+    const bool wt = (S.wmask >> ch) & 1u;
+    // median(), src/chrono.rs:582-591; weight-0 channels keep 0 (chrono.rs:222, :239)
+    r.med[ch] = !wt ? 0.0f
+                    : (S.med_pair ? __fmul_rn(0.5f, __fadd_rn(static_cast<float>(lo),
+                                                              static_cast<float>(hi)))
+                                  : static_cast<float>(lo));
+    r.medo[ch] = __fadd_rn(r.med[ch], 4194304.0f);  // exact: med is a multiple of 1/2
+    r.wi[ch] = rel ? A.wi[q >> 2][q & 3][t] : S.w[ch];
+    const uint32_t s2 = lo + hi;
+    const uint32_t fl = S.med_pair ? (s2 >> 1) : lo, ce = S.med_pair ? ((s2 + 1) >> 1) : lo;
+    if (wt) {
+      r.klo |= fl << (8 * ch);
+      r.khi |= ce << (8 * ch);
+      r.nh += static_cast<int>(ce - fl);
     }
   }
+  return r;
+}
+
+// Stores the tile's staged output rows (C words per column) with coalesced 32-bit stores;
+// a partial or misaligned tile stores its valid bytes one by one.
+template <int C>
+DEVI void store_rows(uint8_t* out, const TileGeo& g, const uint32_t (&rows)[C][32]) {
+  const uint8_t* src = reinterpret_cast<const uint8_t*>(rows);
+  uint8_t* dst = out + static_cast<size_t>(g.out_px0) * C;
+  const int nbytes = g.npx * C;
+  const bool full = nbytes == kTilePx * C && (reinterpret_cast<uintptr_t>(dst) & 3) == 0;
+  for (int i = threadIdx.x; i < 32 * C; i += 32 * C) {
+    // word i of the row: column i / C, word i % C
+    const uint32_t v = rows[i % C][i / C];
+    if (full) {
+      reinterpret_cast<uint32_t*>(dst)[i] = v;
+    } else {
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if (4 * i + b < nbytes) dst[4 * i + b] = static_cast<uint8_t>(v >> (8 * b));
+    }
+  }
+  (void)src;
 }
 
 // ---- the outlier tile -----------------------------------------------------------------------
 template <int C, int NW, bool SH>
 DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
-                       uint32_t& warn_count) {
+                       Aux<C, NW>& A, uint32_t& warn_count) {
   constexpr int BP = NW <= 2 ? 4 : 2;  // byte positions per plane build (register budget)
-  constexpr int NPOS = 4 * C;          // channel bytes of this thread's 4 pixels
-  constexpr int NCH = NPOS / BP;
   const int n = S.n;
-  const int tid = static_cast<int>(threadIdx.x);
+  const int wp = static_cast<int>(threadIdx.x) >> 5;  // warp: word, frame class, pixels
+  const int t = static_cast<int>(threadIdx.x) & 31;   // column
   uint32_t smask[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
   const bool rel = !S.thr_abs;
 
-  // (2)+(3): planes and order statistics, BP positions per round. Results are shifted into
-  // byte (and float) shift registers so that the rolled loop needs no indexed registers.
-  uint32_t lo_sr[C], hi_sr[C];
-  float wi_sr[NPOS];
+  // (2)+(3) planes and order statistics of word wp, BP positions per round
+  {
+    uint32_t plo = 0u, phi = 0u;
+    float wq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-  for (int i = 0; i < C; ++i) lo_sr[i] = hi_sr[i] = 0u;
-#pragma unroll
-  for (int i = 0; i < NPOS; ++i) wi_sr[i] = 0.0f;
-#pragma unroll 1
-  for (int chunk = 0; chunk < NCH; ++chunk) {
-    const int w = (chunk * BP) >> 2, kp0 = (chunk * BP) & 3;
-    uint32_t P[BP][8][NW];
-    build_planes<C, NW, BP, SH>(P, rd, w, kp0, n);
-    uint32_t lo[BP], hi[BP];
-    select_multi<NW, BP>(P, smask, S.med_k, S.med_pair != 0, lo, hi);
-    uint32_t plo = 0, phi = 0;
-#pragma unroll
-    for (int k = 0; k < BP; ++k) {
-      plo |= lo[k] << (8 * k);
-      phi |= hi[k] << (8 * k);
-    }
-    if constexpr (BP == 4) {
-#pragma unroll
-      for (int i = 0; i + 1 < C; ++i) {
-        lo_sr[i] = lo_sr[i + 1];
-        hi_sr[i] = hi_sr[i + 1];
-      }
-      lo_sr[C - 1] = plo;
-      hi_sr[C - 1] = phi;
-    } else {
-#pragma unroll
-      for (int i = 0; i + 1 < C; ++i) {
-        lo_sr[i] = __funnelshift_r(lo_sr[i], lo_sr[i + 1], 16);
-        hi_sr[i] = __funnelshift_r(hi_sr[i], hi_sr[i + 1], 16);
-      }
-      lo_sr[C - 1] = (lo_sr[C - 1] >> 16) | (plo << 16);
-      hi_sr[C - 1] = (hi_sr[C - 1] >> 16) | (phi << 16);
-    }
-    if (rel) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
-      uint32_t a1[BP], b1[BP], a3[BP], b3[BP];
-      select_multi<NW, BP>(P, smask, S.q1_k, S.q1_pair != 0, a1, b1);
-      select_multi<NW, BP>(P, smask, S.q3_k, S.q3_pair != 0, a3, b3);
-      float wnew[BP];
+    for (int kp0 = 0; kp0 < 4; kp0 += BP) {
+      uint32_t P[BP][8][NW];
+      build_planes<C, NW, BP, SH>(P, rd, wp, kp0, n);
+      uint32_t lo[BP], hi[BP];
+      select_multi<NW, BP>(P, smask, S.med_k, S.med_pair != 0, lo, hi);
 #pragma unroll
       for (int k = 0; k < BP; ++k) {
-        const float q1 = quantile_value(a1[k], b1[k], S.q1_pair != 0, S.q1_frac);
-        const float q3 = quantile_value(a3[k], b3[k], S.q3_pair != 0, S.q3_frac);
-        float iqr = __fsub_rn(q3, q1);
-        if (iqr == 0.0f) iqr = 1.0f;
-        const int q = chunk * BP + k, ch = q % C;
-        wnew[k] = __fmul_rn(S.w[ch], __fdiv_rn(1.0f, iqr));
-        const int px = g.out_px0 + 4 * tid + q / C;
-        if ((S.dbg_q1 || S.dbg_q3) && 4 * tid + q / C < g.npx) {
-          const bool wt = (S.wmask >> ch) & 1u;
-          if (S.dbg_q1) S.dbg_q1[static_cast<size_t>(px) * C + ch] = wt ? q1 : 0.0f;
-          if (S.dbg_q3) S.dbg_q3[static_cast<size_t>(px) * C + ch] = wt ? q3 : 0.0f;
+        plo |= lo[k] << (8 * (kp0 + k));
+        phi |= hi[k] << (8 * (kp0 + k));
+      }
+      if (rel) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
+        uint32_t a1[BP], b1[BP], a3[BP], b3[BP];
+        select_multi<NW, BP>(P, smask, S.q1_k, S.q1_pair != 0, a1, b1);
+        select_multi<NW, BP>(P, smask, S.q3_k, S.q3_pair != 0, a3, b3);
+#pragma unroll
+        for (int k = 0; k < BP; ++k) {
+          const float q1 = quantile_value(a1[k], b1[k], S.q1_pair != 0, S.q1_frac);
+          const float q3 = quantile_value(a3[k], b3[k], S.q3_pair != 0, S.q3_frac);
+          float iqr = __fsub_rn(q3, q1);
+          if (iqr == 0.0f) iqr = 1.0f;
+          const int q = 4 * wp + kp0 + k, ch = q % C;
+          wq[kp0 + k] = __fmul_rn(S.w[ch], __fdiv_rn(1.0f, iqr));
+          const int px = 4 * t + q / C;
+          if ((S.dbg_q1 || S.dbg_q3) && px < g.npx) {
+            const size_t o = static_cast<size_t>(g.out_px0 + px) * C + ch;
+            const bool wt = (S.wmask >> ch) & 1u;
+            if (S.dbg_q1) S.dbg_q1[o] = wt ? q1 : 0.0f;
+            if (S.dbg_q3) S.dbg_q3[o] = wt ? q3 : 0.0f;
+          }
         }
       }
-#pragma unroll
-      for (int i = 0; i + BP < NPOS; ++i) wi_sr[i] = wi_sr[i + BP];
-#pragma unroll
-      for (int k = 0; k < BP; ++k) wi_sr[NPOS - BP + k] = wnew[k];
     }
+    A.lo[wp][t] = plo;
+    A.hi[wp][t] = phi;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) A.wi[wp][k][t] = wq[k];
   }
+  __syncthreads();
 
-  // per-pixel statistics from the shift registers (compile-time positions)
-  uint32_t klo[4], khi[4];
-  int nh[4];
-  float med[4][C], medo[4][C], wi[4][C];
-#pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    klo[p] = khi[p] = 0u;
-    nh[p] = 0;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) {
-      const int q = p * C + ch;
-      const uint32_t lo = (lo_sr[q >> 2] >> (8 * (q & 3))) & 0xFFu;
-      const uint32_t hi = (hi_sr[q >> 2] >> (8 * (q & 3))) & 0xFFu;
-      const bool wt = (S.wmask >> ch) & 1u;
-      // median(), src/chrono.rs:582-591; weight-0 channels keep 0 (chrono.rs:222, :239)
-      med[p][ch] = !wt ? 0.0f
-                       : (S.med_pair ? __fmul_rn(0.5f, __fadd_rn(static_cast<float>(lo),
-                                                                 static_cast<float>(hi)))
-                                     : static_cast<float>(lo));
-      medo[p][ch] = __fadd_rn(med[p][ch], 4194304.0f);  // exact: med is a multiple of 1/2
-      wi[p][ch] = rel ? wi_sr[q] : S.w[ch];
-      const uint32_t s2 = lo + hi;
-      const uint32_t fl = S.med_pair ? (s2 >> 1) : lo, ce = S.med_pair ? ((s2 + 1) >> 1) : lo;
-      if (wt) {
-        klo[p] |= fl << (8 * ch);
-        khi[p] |= ce << (8 * ch);
-        nh[p] += static_cast<int>(ce - fl);
-      }
-    }
-  }
-  if (S.dbg_median) {
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-      if (4 * tid + p < g.npx)
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch)
-          S.dbg_median[static_cast<size_t>(g.out_px0 + 4 * tid + p) * C + ch] = med[p][ch];
-  }
-
-  // (4) distance pass over all frames (src/chrono.rs:261-288)
+  // per-pixel statistics of this column
   const bool fast = S.fast_int != 0;
   uint32_t wbytes = 0;
 #pragma unroll
   for (int ch = 0; ch < C; ++ch)
     if ((S.wmask >> ch) & 1u) wbytes |= 0xFFu << (8 * ch);
-  uint32_t bits[4][NW];
-  int imax[4];
-  int32_t dmax_i[4];
-  float dmax_f[4];
-  int32_t thr_i[4];
-  int32_t kmax[4];
+  uint32_t klo[4], khi[4];
+  int nh[4];
+  float medo[4][C], wi[4][C];
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
-    imax[p] = 0;
-    dmax_i[p] = 0;
-    // max key (D' << 8) + 255 - f; the reference starts from dist_sq 0.0 at frame 0 and
-    // takes strictly larger values: with nh > 0 every frame beats that start (-1)
-    kmax[p] = nh[p] > 0 ? -1 : 255;
-    dmax_f[p] = 0.0f;
-    thr_i[p] = S.thr_int[nh[p]];
+    const PixStats<C> ps = pixel_stats<C, NW>(S, A, t, p);
+    klo[p] = ps.klo;
+    khi[p] = ps.khi;
+    nh[p] = ps.nh;
 #pragma unroll
-    for (int w = 0; w < NW; ++w) bits[p][w] = 0u;
-  }
-#pragma unroll
-  for (int blk = 0; blk < NW; ++blk) {
-    const int f0 = blk * 32;
-    const int fend = min(n, f0 + 32);
-    uint32_t ob[4] = {0u, 0u, 0u, 0u};
-    if (fast) {
-#pragma unroll kDistUnroll
-      for (int f = f0; f < fend; ++f) {
-        uint32_t wv[C];
-        rd.frame(f, wv);
-        const uint32_t m = 1u << (f - f0);
-        const int32_t fk = 255 - f;
-#pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          const int32_t d =
-              static_cast<int32_t>(dist_int(pixel_word<C>(wv, p), wbytes, klo[p], khi[p]));
-          ob[p] |= d >= thr_i[p] ? m : 0u;
-          // the largest distance, earliest frame first: the argmax over all frames is an
-          // outlier whenever any frame is one (src/chrono.rs:283-286)
-          kmax[p] = max(kmax[p], (d << 8) + fk);
-        }
-      }
-    } else if (S.finite_w) {
-      for (int f = f0; f < fend; ++f) {
-        uint32_t wv[C];
-        rd.frame(f, wv);
-        const uint32_t m = 1u << (f - f0);
-#pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          const float d = dist_f32<C, true>(S, medo[p], wi[p], pixel_word<C>(wv, p));
-          const bool o = d >= S.thr_sq;
-          ob[p] |= o ? m : 0u;
-          const bool up = o && d > dmax_f[p];
-          dmax_f[p] = up ? d : dmax_f[p];
-          imax[p] = up ? f : imax[p];
-        }
-      }
-    } else {
-      for (int f = f0; f < fend; ++f) {
-        uint32_t wv[C];
-        rd.frame(f, wv);
-        const uint32_t m = 1u << (f - f0);
-#pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          const float d = dist_f32<C, false>(S, medo[p], wi[p], pixel_word<C>(wv, p));
-          const bool o = d >= S.thr_sq;
-          ob[p] |= o ? m : 0u;
-          const bool up = o && d > dmax_f[p];
-          dmax_f[p] = up ? d : dmax_f[p];
-          imax[p] = up ? f : imax[p];
-        }
-      }
+    for (int ch = 0; ch < C; ++ch) {
+      medo[p][ch] = ps.medo[ch];
+      wi[p][ch] = ps.wi[ch];
     }
-#pragma unroll
-    for (int p = 0; p < 4; ++p) bits[p][blk] = ob[p];
   }
-  if (fast) {
+  if (S.dbg_median && wp == 0) {
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      dmax_i[p] = kmax[p] < 0 ? -1 : (kmax[p] >> 8);
-      imax[p] = kmax[p] < 0 ? 0 : 255 - (kmax[p] & 255);
-    }
+    for (int p = 0; p < 4; ++p)
+      if (4 * t + p < g.npx) {
+        const PixStats<C> ps = pixel_stats<C, NW>(S, A, t, p);
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch)
+          S.dbg_median[static_cast<size_t>(g.out_px0 + 4 * t + p) * C + ch] = ps.med[ch];
+      }
   }
 
-  // (5) per-pixel epilogue, src/chrono.rs:290-493, rolled over the 4 pixels
-  uint32_t outw[4] = {0u, 0u, 0u, 0u}, maskb[4] = {0u, 0u, 0u, 0u};
-#pragma unroll 1
-  for (int p = 0; p < 4; ++p) {
-    const int pix_idx = g.out_px0 + 4 * tid + p;
-    const bool valid = 4 * tid + p < g.npx;
-    uint32_t pb[NW];
+  // (4) distance pass (src/chrono.rs:261-288) over the frames f = wp (mod C)
+  {
+    uint32_t bits[4][NW];
+    int32_t kmax[4], thr_i[4], imax[4];
+    float dmax_f[4];
 #pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      uint32_t v = bits[0][w];
-      v = p == 1 ? bits[1][w] : v;
-      v = p == 2 ? bits[2][w] : v;
-      v = p == 3 ? bits[3][w] : v;
-      pb[w] = v;
+    for (int p = 0; p < 4; ++p) {
+      // max key (D' << 8) + 255 - f; the reference starts from dist_sq 0.0 at frame 0 and
+      // takes strictly larger values: with nh > 0 every frame beats that start (-1)
+      kmax[p] = nh[p] > 0 ? -1 : 255;
+      thr_i[p] = S.thr_int[nh[p]];
+      dmax_f[p] = 0.0f;
+      imax[p] = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) bits[p][w] = 0u;
     }
-    const uint32_t pklo = pick4(klo, p), pkhi = pick4(khi, p);
-    const int pnh = pick4(nh, p);
+#pragma unroll
+    for (int blk = 0; blk < NW; ++blk) {
+      const int f0 = blk * 32;
+      const int fend = min(n, f0 + 32);
+      int fs = f0 + ((wp - f0 % C) % C + C) % C;  // first frame of class wp in the block
+      uint32_t ob[4] = {0u, 0u, 0u, 0u};
+      if (fast) {
+#pragma unroll 2
+        for (int f = fs; f < fend; f += C) {
+          uint32_t wv[C];
+          rd.frame(f, wv);
+          const uint32_t m = 1u << (f - f0);
+          const int32_t fk = 255 - f;
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            const int32_t d =
+                static_cast<int32_t>(dist_int(pixel_word<C>(wv, p), wbytes, klo[p], khi[p]));
+            ob[p] |= d >= thr_i[p] ? m : 0u;
+            // the largest distance, earliest frame first: the argmax over all frames is an
+            // outlier whenever any frame is one (src/chrono.rs:283-286)
+            kmax[p] = max(kmax[p], (d << 8) + fk);
+          }
+        }
+      } else if (S.finite_w) {
+        for (int f = fs; f < fend; f += C) {
+          uint32_t wv[C];
+          rd.frame(f, wv);
+          const uint32_t m = 1u << (f - f0);
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            const float d = dist_f32<C, true>(S, medo[p], wi[p], pixel_word<C>(wv, p));
+            const bool o = d >= S.thr_sq;
+            ob[p] |= o ? m : 0u;
+            const bool up = o && d > dmax_f[p];
+            dmax_f[p] = up ? d : dmax_f[p];
+            imax[p] = up ? f : imax[p];
+          }
+        }
+      } else {
+        for (int f = fs; f < fend; f += C) {
+          uint32_t wv[C];
+          rd.frame(f, wv);
+          const uint32_t m = 1u << (f - f0);
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            const float d = dist_f32<C, false>(S, medo[p], wi[p], pixel_word<C>(wv, p));
+            const bool o = d >= S.thr_sq;
+            ob[p] |= o ? m : 0u;
+            const bool up = o && d > dmax_f[p];
+            dmax_f[p] = up ? d : dmax_f[p];
+            imax[p] = up ? f : imax[p];
+          }
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p) bits[p][blk] = ob[p];
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+#pragma unroll
+      for (int w = 0; w < NW; ++w) A.bits[wp][p][w][t] = bits[p][w];
+      A.best[wp][p][t] = fast ? kmax[p] : __float_as_int(dmax_f[p]);
+      A.imf[wp][p][t] = imax[p];
+    }
+  }
+  __syncthreads();
+
+  // (5) per-pixel epilogue, src/chrono.rs:290-493: warp wp takes pixels wp, wp + C, ...
+#pragma unroll 1
+  for (int p = wp; p < 4; p += C) {
+    const int pix_idx = g.out_px0 + 4 * t + p;
+    const bool valid = 4 * t + p < g.npx;
+    // combine the frame classes: flags OR, integer key max, f32 (distance, earliest frame)
+    uint32_t pb[NW];
+    int32_t key = A.best[0][p][t];
+    float pdmax_f = __int_as_float(A.best[0][p][t]);
+    int pimf = A.imf[0][p][t];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) pb[w] = A.bits[0][p][w][t];
+#pragma unroll
+    for (int c = 1; c < C; ++c) {
+#pragma unroll
+      for (int w = 0; w < NW; ++w) pb[w] |= A.bits[c][p][w][t];
+      key = max(key, A.best[c][p][t]);
+      const float d = __int_as_float(A.best[c][p][t]);
+      const int fi = A.imf[c][p][t];
+      const bool better = d > pdmax_f || (d == pdmax_f && fi < pimf);
+      pdmax_f = better ? d : pdmax_f;
+      pimf = better ? fi : pimf;
+    }
+    const PixStats<C> ps = pixel_stats<C, NW>(S, A, t, p);
+    const uint32_t pklo = ps.klo, pkhi = ps.khi;
+    const int pnh = ps.nh;
     float pmed[C], pmedo[C], pwi[C];
 #pragma unroll
     for (int ch = 0; ch < C; ++ch) {
-      float m = med[0][ch], q = wi[0][ch], mo = medo[0][ch];
-      m = p == 1 ? med[1][ch] : m;
-      m = p == 2 ? med[2][ch] : m;
-      m = p == 3 ? med[3][ch] : m;
-      mo = p == 1 ? medo[1][ch] : mo;
-      mo = p == 2 ? medo[2][ch] : mo;
-      mo = p == 3 ? medo[3][ch] : mo;
-      pmedo[ch] = mo;
-      q = p == 1 ? wi[1][ch] : q;
-      q = p == 2 ? wi[2][ch] : q;
-      q = p == 3 ? wi[3][ch] : q;
-      pmed[ch] = m;
-      pwi[ch] = q;
+      pmed[ch] = ps.med[ch];
+      pmedo[ch] = ps.medo[ch];
+      pwi[ch] = ps.wi[ch];
     }
+    const int pimax = fast ? (key < 0 ? 0 : 255 - (key & 255)) : pimf;
+    const int32_t pdmax_i = key < 0 ? -1 : (key >> 8);
     auto dsq_px = [&](uint32_t px) -> float {  // dist_sq of a sample, recomputed
       if (fast)
         return static_cast<float>(dist_int(px, wbytes, pklo, pkhi)) +
@@ -848,12 +857,12 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
       int si;
       float dsq;
       if (S.outlier == CP_OUTLIER_EXTREME) {
-        si = pick4(imax, p);
+        si = pimax;
         if (fast) {
-          const int32_t dm = pick4(dmax_i, p);
+          const int32_t dm = pdmax_i;
           dsq = dm < 0 ? 0.0f : static_cast<float>(dm) + 0.25f * static_cast<float>(pnh);
         } else {
-          dsq = pick4(dmax_f, p);
+          dsq = pdmax_f;
         }
       } else {
         si = S.outlier == CP_OUTLIER_LAST ? last_set<NW>(pb) : first_set<NW>(pb);
@@ -950,10 +959,15 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
         chosen = si;
       }
     }
+    // stage the pixel's composite and mask bytes (255 in channels >= 3, chrono.rs:183-191)
+    uint8_t* ob = reinterpret_cast<uint8_t*>(A.out);
+    uint8_t* bb = reinterpret_cast<uint8_t*>(A.blend);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      outw[q] = q == p ? pix : outw[q];
-      maskb[q] = q == p ? mask : maskb[q];
+    for (int ch = 0; ch < C; ++ch) {
+      const int q = p * C + ch;  // byte q of column t = word q/4 byte q%4
+      const int off = 4 * (32 * (q >> 2) + t) + (q & 3);
+      ob[off] = static_cast<uint8_t>(pix >> (8 * ch));
+      bb[off] = static_cast<uint8_t>(ch < 3 ? mask : 255u);
     }
     if (valid) {
       if (warning) warn_count += 1;
@@ -968,86 +982,62 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
       if (S.dbg_nout) S.dbg_nout[pix_idx] = nout;
     }
   }
-  store_pixels<C>(S.out, g, tid, outw);
-  if (S.blend) {
-    uint32_t bm[4];
-#pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      uint32_t v = 0;
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) v |= (ch < 3 ? maskb[p] : 255u) << (8 * ch);
-      bm[p] = v;
-    }
-    store_pixels<C>(S.blend, g, tid, bm);  // blend mask, 255 in channels >= 3 (chrono.rs:183-191)
-  }
+  __syncthreads();
+  store_rows<C>(S.out, g, A.out);
+  if (S.blend) store_rows<C>(S.blend, g, A.blend);
 }
 
 // ---- darker / lighter tile ----------------------------------------------------------------
-// SimpleProcessor fold, src/simple.rs:96-133: running extreme of sum_c p_c * w_c (f32, c
-// ascending, strict compare: the earliest frame wins ties); on a new extreme the frame's
-// pixel is blended into the running output (starting at 0) with the frame's fade.
-template <int C, bool SH>
-DEVI void simple_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd) {
+// SimpleProcessor fold, src/simple.rs:96-133, for stacks the streaming kernel does not take
+// (cropped or unaligned frames): running extreme of sum_c p_c * w_c (f32, c ascending, strict
+// compare: the earliest frame wins ties); on a new extreme the frame's pixel is blended into
+// the running output (starting at 0) with the frame's fade. Warp wp takes pixels wp, wp+C, ...
+template <int C, int NW, bool SH>
+DEVI void simple_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd, Aux<C, NW>& A) {
   const bool darker = S.mode == CP_MODE_DARKER;
-  const int tid = static_cast<int>(threadIdx.x);
-  uint32_t outw[4] = {0u, 0u, 0u, 0u};
-  if (S.unit_w && S.no_fade) {
-    // weights 0/1: the f32 sum is an exact integer; every fade is >= 1: copy on a new extreme
-    uint32_t wbytes = 0;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch)
-      if ((S.wmask >> ch) & 1u) wbytes |= 0xFFu << (8 * ch);
-    int32_t ext[4];
-#pragma unroll
-    for (int p = 0; p < 4; ++p) ext[p] = darker ? 0x7FFFFFFF : -1;
-#pragma unroll 4
+  const int wp = static_cast<int>(threadIdx.x) >> 5;
+  const int t = static_cast<int>(threadIdx.x) & 31;
+#pragma unroll 1
+  for (int p = wp; p < 4; p += C) {
+    float ext = darker ? FLT_MAX : -FLT_MAX;
+    uint32_t outw = 0u;
     for (int f = 0; f < S.n; ++f) {
-      uint32_t wv[C];
-      rd.frame(f, wv);
+      const uint32_t px = load_pixel<C, SH>(rd, f, p);
+      float value = 0.0f;
 #pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        const uint32_t px = pixel_word<C>(wv, p);
-        const int32_t v = static_cast<int32_t>(__dp4a(px & wbytes, 0x01010101u, 0u));
-        const bool up = darker ? v < ext[p] : v > ext[p];
-        ext[p] = up ? v : ext[p];
-        outw[p] = up ? px : outw[p];
-      }
-    }
-  } else {
-    float ext[4];
-#pragma unroll
-    for (int p = 0; p < 4; ++p) ext[p] = darker ? FLT_MAX : -FLT_MAX;
-    for (int f = 0; f < S.n; ++f) {
-      uint32_t wv[C];
-      rd.frame(f, wv);
+      for (int ch = 0; ch < C; ++ch)
+        value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
+      const bool up = darker ? (value < ext) : (value > ext);
+      ext = up ? value : ext;
       const float fade = S.fade[f];
+      if (up && fade > 0.0f) outw = fade >= 1.0f ? px : blend_into_u8<C>(outw, px, fade);
+    }
+    uint8_t* ob = reinterpret_cast<uint8_t*>(A.out);
 #pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        const uint32_t px = pixel_word<C>(wv, p);
-        float value = 0.0f;
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch)
-          value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
-        const bool up = darker ? (value < ext[p]) : (value > ext[p]);
-        ext[p] = up ? value : ext[p];
-        if (up && fade > 0.0f) outw[p] = fade >= 1.0f ? px : blend_into_u8<C>(outw[p], px, fade);
-      }
+    for (int ch = 0; ch < C; ++ch) {
+      const int q = p * C + ch;
+      ob[4 * (32 * (q >> 2) + t) + (q & 3)] = static_cast<uint8_t>(outw >> (8 * ch));
     }
   }
-  store_pixels<C>(S.out, g, tid, outw);
+  __syncthreads();
+  store_rows<C>(S.out, g, A.out);
 }
 
 template <int C, bool SH>
 DEVI void process_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
-                       uint32_t& warn) {
-  if (S.mode != CP_MODE_OUTLIER) {
-    simple_tile<C, SH>(S, g, rd);
-  } else if (S.nw == 1) {
-    outlier_tile<C, 1, SH>(S, g, rd, warn);
+                       uint8_t* aux, uint32_t& warn) {
+  if (S.nw == 1) {
+    Aux<C, 1>& A = *reinterpret_cast<Aux<C, 1>*>(aux);
+    if (S.mode != CP_MODE_OUTLIER) simple_tile<C, 1, SH>(S, g, rd, A);
+    else outlier_tile<C, 1, SH>(S, g, rd, A, warn);
   } else if (S.nw == 2) {
-    outlier_tile<C, 2, SH>(S, g, rd, warn);
+    Aux<C, 2>& A = *reinterpret_cast<Aux<C, 2>*>(aux);
+    if (S.mode != CP_MODE_OUTLIER) simple_tile<C, 2, SH>(S, g, rd, A);
+    else outlier_tile<C, 2, SH>(S, g, rd, A, warn);
   } else {
-    outlier_tile<C, 4, SH>(S, g, rd, warn);
+    Aux<C, 4>& A = *reinterpret_cast<Aux<C, 4>*>(aux);
+    if (S.mode != CP_MODE_OUTLIER) simple_tile<C, 4, SH>(S, g, rd, A);
+    else outlier_tile<C, 4, SH>(S, g, rd, A, warn);
   }
 }
 
@@ -1059,24 +1049,33 @@ DEVI void flush_warnings(unsigned long long* dst, uint32_t w) {
 
 struct SmemLayout {
   uint64_t* bar;
-  uint8_t* shifts;
+  uint8_t* shifts;    // [CP_MAX_FRAMES]
+  uintptr_t* fbase;   // [CP_MAX_FRAMES] frame base pointers of the current stack
   uint8_t* buf;
 };
 DEVI SmemLayout smem_layout(uint8_t* smem) {
   SmemLayout l;
   l.bar = reinterpret_cast<uint64_t*>(smem);
   l.shifts = smem + 16;
+  l.fbase = reinterpret_cast<uintptr_t*>(smem + 256);
   l.buf = smem + kSmemHeader;
   return l;
 }
+// Warp 0 copies the stack's frame pointers into shared memory (once per stack).
+DEVI void load_fbase(const StackDev& S, const SmemLayout& L) {
+  if (threadIdx.x < 32)
+    for (int f = threadIdx.x; f < S.n; f += 32)
+      L.fbase[f] = reinterpret_cast<uintptr_t>(S.frames[f]);
+}
 
 // Stage a tile, wait for it (bounded) and process it. Returns false after a timed-out wait.
+// The exchange area sits behind the n staged rows.
 template <int C>
 DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uint32_t& phase,
                    uint32_t* error, uint32_t& warn) {
   if (threadIdx.x < 32) {
     fence_proxy_async();
-    issue_tile<C>(S, g, L.buf, L.shifts, L.bar);
+    issue_tile<C>(S, g, L.buf, L.shifts, L.fbase, L.bar);
   }
   __syncthreads();
   if (!mbar_wait(L.bar, phase)) {
@@ -1084,28 +1083,30 @@ DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uin
     return false;
   }
   phase ^= 1u;
-  const uint8_t* col = L.buf + 4 * C * threadIdx.x;
+  const uint8_t* col = L.buf + 4 * C * (threadIdx.x & 31);
+  uint8_t* aux = L.buf + static_cast<size_t>(S.n) * kPitch<C>;
   if (S.shifted) {
     const Rows<C, true> rd{col, L.shifts};
-    process_tile<C, true>(S, g, rd, warn);
+    process_tile<C, true>(S, g, rd, aux, warn);
   } else {
     const Rows<C, false> rd{col, L.shifts};
-    process_tile<C, false>(S, g, rd, warn);
+    process_tile<C, false>(S, g, rd, aux, warn);
   }
   __syncthreads();
   return true;
 }
 
-// One stack, persistent CTAs striding over its tiles.
+// One stack, persistent CTAs (C warps each) striding over its tiles.
 template <int C>
-__global__ void __launch_bounds__(kThreads) k_composite(const __grid_constant__ StackDev S,
-                                                        uint32_t* error) {
+__global__ void __launch_bounds__(32 * C, 5) k_composite(const __grid_constant__ StackDev S,
+                                                      uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
   const SmemLayout L = smem_layout(smem);
   if (threadIdx.x == 0) {
     mbar_init(L.bar, 1);
     fence_mbar_init();
   }
+  load_fbase(S, L);
   __syncthreads();
   uint32_t phase = 0, warn = 0;
   for (int t = blockIdx.x; t < S.tiles; t += gridDim.x)
@@ -1115,11 +1116,11 @@ __global__ void __launch_bounds__(kThreads) k_composite(const __grid_constant__ 
 
 // Many stacks: persistent CTAs pull (stack, tile) items from a device counter.
 template <int C>
-__global__ void __launch_bounds__(kThreads) k_composite_batch(const StackDev* __restrict__ stacks,
-                                                              const int32_t* __restrict__ prefix,
-                                                              int32_t n_stacks, int32_t total,
-                                                              int32_t interleave,
-                                                              uint32_t* counter, uint32_t* error) {
+__global__ void __launch_bounds__(32 * C, 5) k_composite_batch(const StackDev* __restrict__ stacks,
+                                                            const int32_t* __restrict__ prefix,
+                                                            int32_t n_stacks, int32_t total,
+                                                            int32_t interleave,
+                                                            uint32_t* counter, uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ int item_s, stack_s;
   const SmemLayout L = smem_layout(smem);
@@ -1129,6 +1130,7 @@ __global__ void __launch_bounds__(kThreads) k_composite_batch(const StackDev* __
   }
   __syncthreads();
   uint32_t phase = 0;
+  int cached = -1;  // stack whose frame bases are in shared memory
   for (;;) {
     if (threadIdx.x == 0) {
       const int it = static_cast<int>(atomicAdd(counter, 1u));
@@ -1152,12 +1154,16 @@ __global__ void __launch_bounds__(kThreads) k_composite_batch(const StackDev* __
     const int tile = item_s, s = stack_s;
     if (tile < 0) break;
     const StackDev& S = stacks[s];
+    if (s != cached) {
+      load_fbase(S, L);
+      cached = s;
+      __syncthreads();
+    }
     uint32_t warn = 0;
     if (!run_tile<C>(S, tile_geo(S, tile), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
   }
 }
-
 
 // darker/lighter streaming over an aligned, uncropped stack (no shared-memory staging): each
 // thread owns 16 pixels, i.e. C 16-byte words of every frame, and folds its frames in order
