@@ -76,8 +76,11 @@ def barrier():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """SM clocks, power and clock-event reasons sampled every 10 ms during the timed region
+    through NVML (libnvidia-ml, read-only queries); nvidia-smi at 200 ms if NVML is absent."""
 
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -85,9 +88,53 @@ class ClockSampler:
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
+        self.nvml = None
+        self.stop = threading.Event()
+        self.samples = []   # (sm_mhz, max_mhz, power_w, reason_bits)
         self.lines = []
 
+    def _nvml_handle(self):
+        nv = ct.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return None, None
+        h = ct.c_void_p()
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.gpu)
+            bus = b"%08X:%02X:%02X.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+            if nv.nvmlDeviceGetHandleByPciBusId_v2(bus, ct.byref(h)) == 0:
+                return nv, h
+        except Exception:
+            pass
+        if nv.nvmlDeviceGetHandleByIndex_v2(ct.c_uint(self.gpu), ct.byref(h)) == 0:
+            return nv, h
+        return None, None
+
+    def _poll(self, nv, h):
+        reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        sm, mx, mw, bits = ct.c_uint(), ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        while not self.stop.is_set():
+            if nv.nvmlDeviceGetClockInfo(h, 1, ct.byref(sm)) == 0:
+                nv.nvmlDeviceGetMaxClockInfo(h, 1, ct.byref(mx))
+                nv.nvmlDeviceGetPowerUsage(h, ct.byref(mw))
+                reasons_fn(h, ct.byref(bits))
+                self.samples.append((sm.value, mx.value, mw.value / 1e3, bits.value))
+            self.stop.wait(0.01)
+
     def __enter__(self):
+        try:
+            nv, h = self._nvml_handle()
+        except Exception:
+            nv, h = None, None
+        if nv is not None:
+            self.nvml = nv
+            self.t = threading.Thread(target=self._poll, args=(nv, h), daemon=True)
+            self.t.start()
+            deadline = time.time() + 2.0
+            while not self.samples and time.time() < deadline:
+                time.sleep(0.002)
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
@@ -95,6 +142,9 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.time() + 5.0
+            while not self.lines and time.time() < deadline:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
@@ -104,6 +154,9 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self.stop.set()
+        if self.nvml is not None:
+            self.t.join(timeout=2)
         if self.proc:
             self.proc.terminate()
             try:
@@ -112,7 +165,14 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, mx, power, reasons = [], None, [], set()
+        for s, m, pw, bits in self.samples:
+            sm.append(float(s))
+            mx = float(m)
+            power.append(pw)
+            for b, nm in self.REASONS.items():
+                if bits & b:
+                    reasons.add(nm)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -121,13 +181,16 @@ class ClockSampler:
             try:
                 sm.append(float(parts[1]))
                 mx = float(parts[2])
+                power.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "power_w": statistics.median(power) if power else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "source": "nvml" if self.nvml is not None else "nvidia-smi"}
 
 
 def measured_peaks():
@@ -150,21 +213,28 @@ def profiled_traffic():
     return None
 
 
-def cpu_sample(threads):
-    """Reference CPU path (oracle restatement) on a band of 32 rows of the same stack, the six
-    variants, all host threads. Returns (Mpx-frames/s, seconds, description)."""
-    from chrono_photo_gb300 import example_data, make_params
+def cpu_band(rows):
+    from chrono_photo_gb300 import example_data
+    return example_data.hd_stack(seed=2, n=N_FRAMES, w=W, h=rows)
+
+
+def cpu_sample(threads, frames, reps=1):
+    """Reference CPU path (the oracle's C++ restatement of the reference) on a band of rows of
+    the same stack: the six variants, `reps` times, on `threads` host threads.
+    Returns (Mpx-frames/s, seconds, description)."""
+    from chrono_photo_gb300 import make_params
     from oracle import oracle
-    rows = 160
-    frames = example_data.hd_stack(seed=2, n=N_FRAMES, w=W, h=rows)
+    rows = frames.shape[1]
+    keep = []
+    params = [make_params(keep=keep, **kw) for _, kw in VARIANTS]
     t0 = time.perf_counter()
-    for _, kw in VARIANTS:
-        keep = []
-        p = make_params(keep=keep, **kw)
-        oracle.composite(frames, p, threads=threads)
+    for _ in range(reps):
+        for p in params:
+            oracle.composite(frames, p, threads=threads)
     dt = time.perf_counter() - t0
-    mpxf = len(VARIANTS) * N_FRAMES * W * rows / 1e6
-    return mpxf / dt, dt, "6 variants on a 64x1920x%d band (%d rows of 1080)" % (rows, rows)
+    mpxf = reps * len(VARIANTS) * N_FRAMES * W * rows / 1e6
+    return mpxf / dt, dt, "%d x 6 variants on a 64x1920x%d band (%d rows of 1080), %d threads" % (
+        reps, rows, rows, threads)
 
 
 def run_reference(args):
@@ -172,13 +242,14 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    frames = cpu_band(160)   # one step: the six variants on 160 rows (~0.25 s on 16 cores)
     for _ in range(args.warmup):
-        cpu_sample(threads)
-    vals = []
+        cpu_sample(threads, frames)
+    t = 0.0
     for _ in range(args.steps):
-        v, dt, desc = cpu_sample(threads)
-        vals.append(v)
-    value = statistics.mean(vals)
+        v, dt, desc = cpu_sample(threads, frames)
+        t += dt
+    value = args.steps * len(VARIANTS) * N_FRAMES * W * 160 / 1e6 / t
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * len(VARIANTS) * MPXF_PER_COMPOSITE / value,
@@ -281,7 +352,7 @@ def run_gpu(args):
     outlier_ms = statistics.mean(per_var[:4])
     achieved = ALGO_BYTES_OUTLIER / (outlier_ms / 1e3) / 1e9
     traffic = profiled_traffic()
-    cpu_v, cpu_dt, cpu_desc = cpu_sample(os.cpu_count() or 1)
+    cpu_v, cpu_dt, cpu_desc = cpu_sample(os.cpu_count() or 1, cpu_band(320), reps=3)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
@@ -305,8 +376,8 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

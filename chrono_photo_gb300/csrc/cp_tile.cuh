@@ -142,6 +142,12 @@ DEVI TileGeo tile_geo(const StackDev& S, int t) {
 template <int C>
 constexpr int kPitch = kTilePx * C + 32;
 
+// Resident CTAs per SM the register allocation is sized for: 6 x 96 threads at <= 112
+// registers for RGB; RGBA (4 warps) is limited to 4 by shared memory at 64 frames anyway;
+// grayscale (1 warp) at 16.
+template <int C>
+constexpr int kMinCtas = C == 3 ? 6 : (C == 4 ? 4 : 16);
+
 // Warp 0 stages the n frame rows of a tile into `buf` (row f at f * pitch) from the frame
 // bases cached in shared memory. A source that is not 16-byte aligned (cropped stacks,
 // unaligned frames) is copied from the aligned address below it and the offset is recorded
@@ -437,9 +443,11 @@ DEVI float dist_f32(const StackDev& S, const float (&medo)[C], const float (&wi)
   return d;
 }
 // Exact integer form for abs thresholds and 0/1 weights: D' with dist_sq = D' + nh/4.
+// Each channel term |p - lo| * |p - hi| = (p - lo) * (p - hi) (hi - lo is 0 or 1 and p is an
+// integer, so the product is never negative) = p*p - p*lo - p*hi + lo*hi: three dp4a.
 DEVI uint32_t dist_int(uint32_t px, uint32_t wbytes, uint32_t klo, uint32_t khi) {
   const uint32_t v = px & wbytes;
-  return __dp4a(__vabsdiffu4(v, klo), __vabsdiffu4(v, khi), 0u);
+  return __dp4a(v, v, __dp4a(klo, khi, 0u)) - __dp4a(v, khi, __dp4a(v, klo, 0u));
 }
 
 // blend_into_u8, src/color.rs:4-16, on a pixel word.
@@ -1098,7 +1106,7 @@ DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uin
 
 // One stack, persistent CTAs (C warps each) striding over its tiles.
 template <int C>
-__global__ void __launch_bounds__(32 * C, 5) k_composite(const __grid_constant__ StackDev S,
+__global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_constant__ StackDev S,
                                                       uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
   const SmemLayout L = smem_layout(smem);
@@ -1116,7 +1124,7 @@ __global__ void __launch_bounds__(32 * C, 5) k_composite(const __grid_constant__
 
 // Many stacks: persistent CTAs pull (stack, tile) items from a device counter.
 template <int C>
-__global__ void __launch_bounds__(32 * C, 5) k_composite_batch(const StackDev* __restrict__ stacks,
+__global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const StackDev* __restrict__ stacks,
                                                             const int32_t* __restrict__ prefix,
                                                             int32_t n_stacks, int32_t total,
                                                             int32_t interleave,
