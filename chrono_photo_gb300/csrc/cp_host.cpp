@@ -192,6 +192,18 @@ int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
     d->thr_scale = 1.0f / (p->thr_max - p->thr_min);
   }
   d->thr_sq = d->thr_min * d->thr_min;  // src/chrono.rs:220
+  // The paired f32 distance pass computes every term on (median - p) / 2, i.e. each term,
+  // sum and threshold scaled by exactly 1/4. Scaling by a power of two commutes with f32
+  // rounding while no value leaves the normal range: nonzero weights within [2^-53, 2^39]
+  // keep |t| = |w * iqr_inv * diff| (iqr_inv <= 2^16, 1/2 <= |diff| <= 255) and t^2 / 4
+  // normal and the three-term sum finite; negative weights (cancelling sums) are excluded.
+  bool pair = finite && !neg && std::isfinite(d->thr_sq) &&
+              (d->thr_sq == 0.0f || d->thr_sq >= std::ldexp(1.0f, -124));
+  for (int c = 0; c < st->channels; ++c) {
+    const float a = std::fabs(p->weights[c]);
+    if (a != 0.0f && !(a >= std::ldexp(1.0f, -53) && a <= std::ldexp(1.0f, 39))) pair = false;
+  }
+  d->pair_f32 = pair ? 1u : 0u;
   for (int nh = 0; nh <= 4; ++nh) {
     // smallest integer D' with D' + nh/4 >= thr_sq (exact in double)
     const double need = static_cast<double>(d->thr_sq) - 0.25 * nh;

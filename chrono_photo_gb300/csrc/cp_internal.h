@@ -74,6 +74,7 @@ struct StackDev {
   uint32_t neg_w;      // some weight negative
   uint32_t unit_w;     // every weight 0 or 1
   uint32_t finite_w;   // every weight finite with |w| < 1e30: w * iqr_inv stays finite
+  uint32_t pair_f32;   // f32 distances may run halved, two pixels per instruction (see host)
   uint32_t no_fade;    // every fade factor >= 1 (darker/lighter copy the pixel)
   float thr_min, thr_max, thr_scale, thr_sq;
   int32_t thr_int[5];  // smallest integer D' with D' + nh/4 >= thr_sq, per nh = 0..4

@@ -83,6 +83,30 @@ DEVI bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return true;
 }
 
+// Paired f32 add / multiply, round to nearest, as PTX with an explicit rounding mode; each
+// lane rounds like __fadd_rn / __fmul_rn. A paired product must not feed a paired sum: the
+// compiler contracted both __fadd2_rn(d, __fmul2_rn(t, t)) and add.rn.f32x2 after
+// mul.rn.f32x2 into a fused multiply-add even with -fmad=false (one ulp off, which breaks
+// ties between equal distances); products are therefore summed with scalar __fadd_rn.
+DEVI unsigned long long f2_bits(float2 v) {
+  return static_cast<unsigned long long>(__float_as_uint(v.x)) |
+         (static_cast<unsigned long long>(__float_as_uint(v.y)) << 32);
+}
+DEVI float2 bits_f2(unsigned long long b) {
+  return make_float2(__uint_as_float(static_cast<uint32_t>(b)),
+                     __uint_as_float(static_cast<uint32_t>(b >> 32)));
+}
+DEVI float2 add2_rn(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return bits_f2(r);
+}
+DEVI float2 mul2_rn(float2 a, float2 b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return bits_f2(r);
+}
+
 // ---- Rust scalar semantics ------------------------------------------------------------------
 // `f32 as u8`: saturating, NaN -> 0.
 DEVI uint32_t sat_u8(float v) {
@@ -674,6 +698,53 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
             kmax[p] = max(kmax[p], (d << 8) + fk);
           }
         }
+      } else if (S.pair_f32) {
+        // pixels (0, 1) and (2, 3) in float2 lanes, every term on (median - p) / 2: the
+        // sample -(2^14 + p/2) is one byte permute of the pixel byte into -2^14's mantissa,
+        // the median 2^14 + median/2 is exact, and their sum is exactly (median - p) / 2.
+        // Terms, sums and the threshold are the reference's values times exactly 1/4.
+        float2 mq[2][C], wq[2][C];
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int ch = 0; ch < C; ++ch) {
+            const float m0 = __fsub_rn(medo[2 * h][ch], 4194304.0f);
+            const float m1 = __fsub_rn(medo[2 * h + 1][ch], 4194304.0f);
+            mq[h][ch] = make_float2(__fadd_rn(__fmul_rn(m0, 0.5f), 16384.0f),
+                                    __fadd_rn(__fmul_rn(m1, 0.5f), 16384.0f));
+            wq[h][ch] = make_float2(wi[2 * h][ch], wi[2 * h + 1][ch]);
+          }
+        const float thr4 = __fmul_rn(S.thr_sq, 0.25f);
+        for (int f = fs; f < fend; f += C) {
+          uint32_t wv[C];
+          rd.frame(f, wv);
+          const uint32_t m = 1u << (f - f0);
+          float2 dq[2] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+#pragma unroll
+          for (int ch = 0; ch < C; ++ch) {
+            if (!((S.wmask >> ch) & 1u)) continue;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int q0 = 2 * h * C + ch, q1 = q0 + C;  // byte of pixel 2h / 2h+1
+              const float2 nv = make_float2(
+                  __uint_as_float(__byte_perm(wv[q0 >> 2], 0xC6800000u, 0x7604u | ((q0 & 3) << 4))),
+                  __uint_as_float(__byte_perm(wv[q1 >> 2], 0xC6800000u, 0x7604u | ((q1 & 3) << 4))));
+              const float2 tt = mul2_rn(wq[h][ch], add2_rn(mq[h][ch], nv));
+              const float2 sq = mul2_rn(tt, tt);
+              dq[h].x = __fadd_rn(dq[h].x, sq.x);
+              dq[h].y = __fadd_rn(dq[h].y, sq.y);
+            }
+          }
+          const float dd[4] = {dq[0].x, dq[0].y, dq[1].x, dq[1].y};
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            const bool o = dd[p] >= thr4;
+            ob[p] |= o ? m : 0u;
+            const bool up = o && dd[p] > dmax_f[p];
+            dmax_f[p] = up ? dd[p] : dmax_f[p];
+            imax[p] = up ? f : imax[p];
+          }
+        }
       } else if (S.finite_w) {
         for (int f = fs; f < fend; f += C) {
           uint32_t wv[C];
@@ -712,7 +783,10 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     for (int p = 0; p < 4; ++p) {
 #pragma unroll
       for (int w = 0; w < NW; ++w) A.bits[wp][p][w][t] = bits[p][w];
-      A.best[wp][p][t] = fast ? kmax[p] : __float_as_int(dmax_f[p]);
+      // the paired pass kept distances / 4: scale back exactly
+      A.best[wp][p][t] =
+          fast ? kmax[p]
+               : __float_as_int(S.pair_f32 ? __fmul_rn(dmax_f[p], 4.0f) : dmax_f[p]);
       A.imf[wp][p][t] = imax[p];
     }
   }
