@@ -373,12 +373,319 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
 
 
+# ---- other configurations (--workload): their own JSON lines, not the headline ---------------
+def _ctx_and_lib():
+    import torch
+    from chrono_photo_gb300 import _abi
+    from chrono_photo_gb300.api import Context
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    return Context(local), _abi.lib(), _abi, local
+
+
+def _pinned(ctx, lib, nbytes):
+    import numpy as np
+    ptr = ct.c_void_p()
+    ctx.check(lib.cp_host_alloc(ctx.handle, nbytes, ct.byref(ptr)))
+    return ptr.value, np.ctypeslib.as_array((ct.c_uint8 * nbytes).from_address(ptr.value))
+
+
+def _time_device(ctx, lib, fn, steps, warmup):
+    """Mean ms per call of fn() on the library's stream (CUDA events), after warm-up."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    ctx.synchronize()
+    stream = torch.cuda.ExternalStream(lib.cp_ctx_stream(ctx.handle))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_video(args):
+    """Chrono-video: 300 resident frames of 1920x1080 (brightness drift, one disk on a sine
+    path), 269 windows [f, f+32) with explicit index lists, abs/0.05/0.2 extreme, background
+    first, all windows in one persistent (graph-replayed) launch per call."""
+    import numpy as np
+    from chrono_photo_gb300 import example_data, make_params
+    ctx, lib, _abi, local = _ctx_and_lib()
+    n_pool, win = 300, 32
+    nwin = n_pool - win + 1
+    fb = W * H * C
+    hptr, host = _pinned(ctx, lib, n_pool * fb)
+    example_data.video_stack(seed=3, n=n_pool, out=host.reshape(n_pool, H, W, C))
+    dev = ctx.alloc(n_pool * fb)
+    ctx.check(lib.cp_memcpy_h2d(ctx.handle, dev, hptr, n_pool * fb, None))
+    frame_ptrs = (ct.c_void_p * n_pool)(*[dev + i * fb for i in range(n_pool)])
+    starts = np.arange(nwin, dtype=np.int64) * win
+    lens = np.full(nwin, win, np.int32)
+    idx = np.concatenate([np.arange(k, k + win, dtype=np.int32) for k in range(nwin)])
+    outs_dev = ctx.alloc(2 * nwin * fb)
+    outs = (ct.c_void_p * nwin)(*[outs_dev + k * fb for k in range(nwin)])
+    blends = (ct.c_void_p * nwin)(*[outs_dev + (nwin + k) * fb for k in range(nwin)])
+    keep = []
+    p = make_params(keep=keep, mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+                    background="first")
+
+    def call():
+        ctx.check(lib.cp_composite_video_device(
+            ctx.handle, frame_ptrs, n_pool, W, H, C, nwin, starts.ctypes.data_as(_abi.I64P),
+            lens.ctypes.data_as(_abi.I32P), idx.ctypes.data_as(_abi.I32P), ct.byref(p), outs,
+            blends, None, None), "cp_composite_video_device")
+
+    with ClockSampler(local) as clk:
+        ms = _time_device(ctx, lib, call, args.steps, args.warmup)
+    # end to end: upload the pool from pinned memory, composite, read every window back
+    optr, _ = _pinned(ctx, lib, 2 * nwin * fb)
+    e2e_steps = max(1, min(args.steps, 10))
+
+    def e2e():
+        ctx.check(lib.cp_memcpy_h2d(ctx.handle, dev, hptr, n_pool * fb, None))
+        call()
+        ctx.check(lib.cp_memcpy_d2h(ctx.handle, optr, outs_dev, 2 * nwin * fb, None))
+        ctx.synchronize()
+    e2e()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    mpxf = nwin * win * W * H / 1e6
+    unique = n_pool * fb + 2 * nwin * fb
+    peaks, kind = measured_peaks()
+    ach = unique / (ms / 1e3) / 1e9
+    print(json.dumps({
+        "workload": "video", "metric": METRIC, "value": mpxf / (ms / 1e3), "unit": METRIC,
+        "ms_per_call": ms, "steps": args.steps, "warmup": args.warmup, "dtype": "u8",
+        "data": "synthetic (seeded drift + sine-path disk)",
+        "config": {"pool": n_pool, "windows": nwin, "window": win, "width": W, "height": H,
+                   "settings": "abs/0.05/0.2 extreme, background first"},
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / peaks["hbm_gbs"], "bytes": unique,
+                     "note": "unique bytes: pool read once + composite and mask per window"},
+        "e2e": {"value": mpxf / e2e_s, "unit": METRIC, "h2d_bytes_per_step": n_pool * fb,
+                "d2h_bytes_per_step": 2 * nwin * fb},
+        "clocks": clk.summary()}), flush=True)
+
+
+SERVE_RES = [(320, 240), (1280, 720), (1920, 1080), (4000, 3000)]
+
+
+def run_serve(args):
+    """Mixed jobs through the continuous-batching server: 512 jobs, N ~ U{8..128},
+    resolution ~ U{320x240, 1280x720, 1920x1080, 4000x3000}, outlier mode ~ U{extreme,
+    average, first, last}, Poisson arrivals, 60 GB HBM budget. Job frames are drawn (by the
+    job's seed) from 16 pinned host frames per resolution, so the host side stays small;
+    every job still uploads its own N frames."""
+    import numpy as np
+    from chrono_photo_gb300 import example_data, make_params
+    from chrono_photo_gb300.api import Server
+    ctx, lib, _abi, local = _ctx_and_lib()
+    jobs = example_data.job_specs(seed=4, count=args.jobs)
+    pool_n = 16
+    pools = {}
+    for (w, h) in SERVE_RES:
+        ptr, arr = _pinned(ctx, lib, pool_n * w * h * C)
+        arr = arr.reshape(pool_n, h, w, C)
+        example_data.stack(pool_n, w, h, sigma=3, n_disks=2, rmin=h / 40, rmax=h / 20,
+                           seed=4 + w, out=arr)
+        pools[(w, h)] = (ptr, arr)
+    mpx_job = [j["n"] * j["w"] * j["h"] / 1e6 for j in jobs]
+
+    def frames_of(j):
+        arr = pools[(j["w"], j["h"])][1]
+        return [arr[(j["seed"] + i) % pool_n] for i in range(j["n"])]
+
+    # kernel only: the same jobs with device-resident frames, 64 per batched launch
+    dpool = {}
+    for key, (ptr, arr) in pools.items():
+        d = ctx.alloc(arr.nbytes)
+        ctx.check(lib.cp_memcpy_h2d(ctx.handle, d, ptr, arr.nbytes, None))
+        dpool[key] = d
+    keep = []
+    params = [make_params(keep=keep, mode="outlier", threshold="abs/0.05/0.2",
+                          outlier=j["outlier"], background="first", seed=j["seed"]) for j in jobs]
+    batches = []
+    for b0 in range(0, len(jobs), 64):
+        bj = list(range(b0, min(b0 + 64, len(jobs))))
+        stacks = (_abi.Stack * len(bj))()
+        outs = (ct.c_void_p * len(bj))()
+        for k, ji in enumerate(bj):
+            j = jobs[ji]
+            fb = j["w"] * j["h"] * C
+            ptrs = (ct.c_void_p * j["n"])(*[dpool[(j["w"], j["h"])] + ((j["seed"] + i) % pool_n) * fb
+                                            for i in range(j["n"])])
+            keep.append(ptrs)
+            stacks[k] = _abi.Stack(n=j["n"], width=j["w"], height=j["h"], channels=C,
+                                   frames=ct.cast(ptrs, ct.POINTER(ct.c_void_p)))
+            outs[k] = ctx.alloc(fb)
+        prm = (_abi.Params * len(bj))(*[params[ji] for ji in bj])
+        batches.append((stacks, prm, outs, len(bj)))
+
+    def kernel_all():
+        for stacks, prm, outs, nb in batches:
+            ctx.check(lib.cp_composite_batch_device(ctx.handle, stacks, prm, nb, outs, None,
+                                                    None, None), "batch")
+    kernel_ms = _time_device(ctx, lib, kernel_all, max(1, args.steps // 50), 1)
+    total_mpxf = sum(mpx_job)
+    kernel_rate = total_mpxf / (kernel_ms / 1e3)
+    # served: Poisson arrivals, mean inter-arrival = 0.5 x the mean kernel-only job time
+    mean_gap = 0.5 * (kernel_ms / 1e3) / len(jobs)
+    rng = np.random.default_rng(4)
+    gaps = rng.exponential(mean_gap, size=len(jobs))
+    with Server(ctx, hbm_budget=60 << 30, max_inflight=8) as srv:
+        warm = srv.submit(frames_of(jobs[0]), params=params[0])
+        srv.wait(warm)
+        ids = []
+        t0 = time.perf_counter()
+        t_next = t0
+        with ClockSampler(local) as clk:
+            for j, g, prm in zip(jobs, gaps, params):
+                t_next += g
+                while time.perf_counter() < t_next:
+                    pass
+                ids.append(srv.submit(frames_of(j), params=prm))
+            res = [srv.wait(i) for i in ids]
+        wall = max(r["done_s"] for r in res) - min(r["submit_s"] for r in res)
+    lat = np.array([r["done_s"] - r["submit_s"] for r in res]) * 1e3
+    bad = sum(1 for r in res if r["status"] != 0)
+    h2d = sum(j["n"] * j["w"] * j["h"] * C for j in jobs)
+    print(json.dumps({
+        "workload": "serve", "metric": METRIC, "value": total_mpxf / wall, "unit": METRIC,
+        "jobs": len(jobs), "failed": bad, "wall_s": wall,
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(lat.max())},
+        "arrival_mean_gap_ms": mean_gap * 1e3,
+        "kernel_only": {"value": kernel_rate, "unit": METRIC, "ms_all_jobs": kernel_ms},
+        "e2e": {"value": total_mpxf / wall, "unit": METRIC, "h2d_bytes_total": h2d,
+                "d2h_bytes_total": 2 * sum(j["w"] * j["h"] * C for j in jobs)},
+        "dtype": "u8", "data": "synthetic (seeded; frames drawn from 16 per resolution)",
+        "config": {"budget_gb": 60, "max_inflight": 8, "settings": "abs/0.05/0.2, background first"},
+        "clocks": clk.summary()}), flush=True)
+
+
+def _shake_frames_device(n, w, h, max_shift, seed):
+    """Seeded shake stack generated on the device (the host generator would take minutes at
+    this size): gradient + 8 random-phase sinusoids, translated per frame by U[-s, s]^2,
+    plus sigma-3 noise and 5 moving disks. Returns (uint8 [n, h, w, 3] tensor, shifts)."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    shifts = rng.integers(-max_shift, max_shift + 1, size=(n, 2))
+    pad = max_shift + 1
+    bw, bh = w + 2 * pad, h + 2 * pad
+    dev = torch.device("cuda")
+    xs = torch.arange(bw, device=dev, dtype=torch.float32)[None, :]
+    ys = torch.arange(bh, device=dev, dtype=torch.float32)[:, None]
+    a = rng.uniform(40, 160, size=3)
+    b = rng.uniform(-40, 40, size=3)
+    d = rng.uniform(-40, 40, size=3)
+    tex = torch.zeros(bh, bw, device=dev)
+    for _ in range(8):
+        fx, fy = rng.uniform(0.04, 0.35, size=2)
+        tex += float(rng.uniform(6, 16)) * torch.sin(float(fx) * xs + float(fy) * ys + float(rng.uniform(0, 6.283)))
+    big = torch.stack([float(a[c]) + float(b[c]) * xs / bw + float(d[c]) * ys / bh + tex
+                       for c in range(3)], dim=-1)
+    out = torch.empty((n, h, w, 3), dtype=torch.uint8, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    disks = [(rng.uniform(0, w), rng.uniform(0.4 * h, 0.6 * h), rng.uniform(0, w),
+              rng.uniform(0.4 * h, 0.6 * h), rng.uniform(20, 60), rng.integers(0, 256, size=3))
+             for _ in range(5)]
+    for i in range(n):
+        dx, dy = int(shifts[i][0]), int(shifts[i][1])
+        f = big[pad + dy:pad + dy + h, pad + dx:pad + dx + w] + \
+            3.0 * torch.randn((h, w, 3), generator=gen, device=dev)
+        t = i / max(n - 1, 1)
+        for (x0, y0, x1, y1, r, col) in disks:
+            cx, cy = x0 + (x1 - x0) * t, y0 + (y1 - y0) * t
+            xa, xb = max(int(cx - r) - 1, 0), min(int(cx + r) + 2, w)
+            ya, yb = max(int(cy - r) - 1, 0), min(int(cy + r) + 2, h)
+            if xa >= xb or ya >= yb:
+                continue
+            yy = torch.arange(ya, yb, device=dev, dtype=torch.float32)[:, None]
+            xx = torch.arange(xa, xb, device=dev, dtype=torch.float32)[None, :]
+            m = (xx - cx) ** 2 + (yy - cy) ** 2 <= r * r
+            f[ya:yb, xa:xb][m] = torch.tensor([float(v) for v in col], device=dev)
+        out[i] = torch.clamp(torch.floor(f + 0.5), 0, 255).to(torch.uint8)
+    torch.cuda.synchronize()
+    return out, shifts
+
+
+def run_shake(args):
+    """Camera shake on 100 frames of 6000x4000: the offset search (4 anchors, radius 32,
+    search radius 20) and the composite of the cropped stack (abs/0.05/0.2 extreme)."""
+    import numpy as np
+    from chrono_photo_gb300 import make_params
+    ctx, lib, _abi, local = _ctx_and_lib()
+    n, w, h, r, s = 100, 6000, 4000, 32, 20
+    frames, shifts = _shake_frames_device(n, w, h, 12, seed=5)
+    fb = w * h * C
+    base = frames.data_ptr()
+    ptrs = (ct.c_void_p * n)(*[base + i * fb for i in range(n)])
+    anchors = np.array([[1000, 800], [5000, 800], [1000, 3200], [5000, 3200]], np.int32)
+    offs = np.zeros((n, 2), np.int32)
+
+    def analyze():
+        ctx.check(lib.cp_shake_analyze_device(ctx.handle, ptrs, n, w, h, C,
+                                              anchors.ctypes.data_as(_abi.I32P), len(anchors), r,
+                                              s, offs.ctypes.data_as(_abi.I32P), None), "shake")
+    with ClockSampler(local) as clk:
+        shake_ms = _time_device(ctx, lib, analyze, max(1, args.steps // 20), 2)
+    expect = shifts[0] - shifts
+    offsets_ok = bool((offs == expect).all())
+    has_crop = ct.c_int32()
+    crops = np.zeros((n, 4), np.int32)   # per frame (x, y, width, height)
+    ctx.check(lib.cp_crop_create(offs.ctypes.data_as(_abi.I32P), n, w, h, ct.byref(has_crop),
+                                 crops.ctypes.data_as(_abi.I32P)), "crop")
+    origins = np.ascontiguousarray(crops[:, :2])
+    cw, ch = (int(crops[0, 2]), int(crops[0, 3])) if has_crop.value else (w, h)
+    keep = []
+    p = make_params(keep=keep, mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+                    background="first")
+    stack = _abi.Stack(n=n, width=cw, height=ch, channels=C,
+                       frames=ct.cast(ptrs, ct.POINTER(ct.c_void_p)),
+                       crop=origins.ctypes.data_as(_abi.I32P) if has_crop.value else None,
+                       src_width=w, src_height=h)
+    out = ctx.alloc(cw * ch * C)
+    blend = ctx.alloc(cw * ch * C)
+
+    def comp():
+        ctx.check(lib.cp_composite_device(ctx.handle, ct.byref(stack), ct.byref(p), out, blend,
+                                          None, None, None), "composite")
+    comp_ms = _time_device(ctx, lib, comp, max(1, args.steps // 20), 2)
+    terms = (n - 1) * len(anchors) * (2 * s + 1) ** 2 * (2 * r + 1) ** 2 * C
+    mpxf = n * cw * ch / 1e6
+    peaks, kind = measured_peaks()
+    algo = n * cw * ch * C + 2 * cw * ch * C
+    print(json.dumps({
+        "workload": "shake", "metric": METRIC, "value": mpxf / (comp_ms / 1e3), "unit": METRIC,
+        "composite_ms": comp_ms, "crop": [cw, ch], "has_crop": int(has_crop.value),
+        "shake": {"ms": shake_ms, "G_ssd_terms_per_s": terms / (shake_ms / 1e3) / 1e9,
+                  "offsets_match_translation": offsets_ok},
+        "roofline": {"bound": "hbm", "achieved": algo / (comp_ms / 1e3) / 1e9,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": algo / (comp_ms / 1e3) / 1e9 / peaks["hbm_gbs"]},
+        "dtype": "u8", "data": "synthetic (seeded, generated on the device)",
+        "config": {"frames": n, "width": w, "height": h, "anchors": anchors.tolist(),
+                   "anchor_radius": r, "search_radius": s},
+        "clocks": clk.summary()}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="hd", choices=["hd", "video", "serve", "shake"],
+                    help="hd (default): the headline line; the others print their own lines")
+    ap.add_argument("--jobs", type=int, default=512, help="serve: number of jobs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, _ = dist_env()
@@ -388,6 +695,12 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args)
+        elif args.workload == "video":
+            run_video(args)
+        elif args.workload == "serve":
+            run_serve(args)
+        elif args.workload == "shake":
+            run_shake(args)
         else:
             run_gpu(args)
     finally:

@@ -381,13 +381,30 @@ class Server:
         self.pending = {}
 
     def submit(self, frames, params=None, keys=None, blend=True, frame_offset=0, **kw):
+        """frames: uint8 [n, h, w, c], or a list of n separate C-contiguous [h, w, c] images
+        (passed by pointer, not copied; they may repeat)."""
         keep = []
         p = params if params is not None else make_params(keep=keep, **kw)
-        a = _as_stack(frames)
-        n, h, w, c = a.shape
         job = _abi.Job()
-        job.stack = _abi.Stack(n=n, width=w, height=h, channels=c, base=a.ctypes.data,
-                               frame_stride=h * w * c, frame_offset=frame_offset)
+        if isinstance(frames, (list, tuple)) and all(
+                isinstance(f, np.ndarray) and f.dtype == np.uint8 and f.flags.c_contiguous
+                for f in frames):
+            a = list(frames)
+            h, w = a[0].shape[:2]
+            c = a[0].shape[2] if a[0].ndim == 3 else 1
+            n = len(a)
+            if any(f.shape != a[0].shape for f in a):
+                raise ValueError("frames differ in shape")
+            ptrs = (ct.c_void_p * n)(*[f.ctypes.data for f in a])
+            keep.append(ptrs)
+            job.stack = _abi.Stack(n=n, width=w, height=h, channels=c,
+                                   frames=ct.cast(ptrs, ct.POINTER(ct.c_void_p)),
+                                   frame_offset=frame_offset)
+        else:
+            a = _as_stack(frames)
+            n, h, w, c = a.shape
+            job.stack = _abi.Stack(n=n, width=w, height=h, channels=c, base=a.ctypes.data,
+                                   frame_stride=h * w * c, frame_offset=frame_offset)
         if keys is not None:
             karr = (ct.c_uint64 * n)(*[int(k) for k in keys])
             keep.append(karr)
