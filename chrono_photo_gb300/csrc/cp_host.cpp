@@ -579,6 +579,7 @@ int cp_ctx_create(int32_t device, uint64_t hbm_budget, cp_ctx** out) {
   ctx->max_smem = static_cast<int>(prop.sharedMemPerBlockOptin);
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->copy_stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking) != cudaSuccess)
     return CP_ERR_CUDA;
   void* p = nullptr;
@@ -595,6 +596,7 @@ void cp_ctx_destroy(cp_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   cudaStreamSynchronize(ctx->copy_stream);
+  cudaStreamSynchronize(ctx->copy_stream2);
   cudaStreamSynchronize(ctx->d2h_stream);
   release_plans(ctx);
   std::vector<void*> ptrs;
@@ -605,6 +607,7 @@ void cp_ctx_destroy(cp_ctx* ctx) {
   for (auto& ev : ctx->band_events) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);
   cudaStreamDestroy(ctx->copy_stream);
+  cudaStreamDestroy(ctx->copy_stream2);
   cudaStreamDestroy(ctx->d2h_stream);
   delete ctx;
 }

@@ -44,6 +44,7 @@ struct cp_ctx {
   int max_smem = 0;
   cudaStream_t stream = nullptr;       // kernels
   cudaStream_t copy_stream = nullptr;  // host -> device staging
+  cudaStream_t copy_stream2 = nullptr; // second host -> device stream (copies alternate)
   cudaStream_t d2h_stream = nullptr;   // device -> host results
   uint64_t budget = 0, used = 0;
   std::mutex mu;      // allocations, budget, caches
