@@ -22,8 +22,10 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-f
               "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
-CU_SOURCES = ["cp_kernels_c1.cu", "cp_kernels_c3.cu", "cp_kernels_c4.cu", "cp_shake.cu",
-              "cp_static.cu"]
+CU_SOURCES = ["cp_kernels_c3.cu", "cp_kernels_c3_int.cu", "cp_kernels_c3_f32.cu",
+              "cp_kernels_c4.cu", "cp_kernels_c4_int.cu", "cp_kernels_c4_f32.cu",
+              "cp_kernels_c1.cu", "cp_kernels_c1_int.cu", "cp_kernels_c1_f32.cu",
+              "cp_shake.cu", "cp_static.cu"]
 CPP_SOURCES = ["cp_host.cpp", "cp_stage.cpp", "cp_batch.cpp", "cp_shake_host.cpp",
                "cp_server.cpp"]
 HEADERS = ["cp_internal.h", "cp_host_internal.h", "cp_tile.cuh"]

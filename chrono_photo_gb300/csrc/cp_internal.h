@@ -102,11 +102,16 @@ inline int smem_bytes_for(int n, int channels) {
   return kSmemHeader + n * row_pitch_host(channels) + aux_bytes(channels, nw_for(n));
 }
 
-// Per-channel-count kernel entry points (cp_kernels_c*.cu). Return cudaError_t values.
+// Per-channel-count kernel entry points (cp_kernels_c*.cu; the integer-distance and f32
+// single-stack kernels in cp_kernels_c*_int.cu / _f32.cu). Return cudaError_t values.
 #define CP_DECLARE_CH(CH)                                                                 \
   int composite_max_ctas_c##CH(int threads, int smem);                                    \
   int launch_composite_c##CH(const StackDev& s, int grid, int smem, void* stream,         \
                              uint32_t* error);                                            \
+  int launch_composite_int_c##CH(const StackDev& s, int grid, int smem, void* stream,     \
+                                 uint32_t* error);                                        \
+  int launch_composite_f32_c##CH(const StackDev& s, int grid, int smem, void* stream,     \
+                                 uint32_t* error);                                        \
   int launch_batch_c##CH(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks, \
                          int32_t total, int32_t interleave, uint32_t* counter,            \
                          uint32_t* error, int grid, int smem, void* stream);              \

@@ -4,7 +4,7 @@
 namespace cp {
 
 int composite_max_ctas_c3(int threads, int smem) {
-  const void* fn = reinterpret_cast<const void*>(&k_composite<3>);
+  const void* fn = reinterpret_cast<const void*>(&k_composite<3, kAnyKind>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess)
@@ -12,11 +12,12 @@ int composite_max_ctas_c3(int threads, int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
+// Outlier stacks go to the kernel of their distance arithmetic, the rest to the general one.
 int launch_composite_c3(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
-  cudaFuncSetAttribute(reinterpret_cast<const void*>(&k_composite<3>),
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_composite<3><<<grid, s.threads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
-  return static_cast<int>(cudaGetLastError());
+  if (s.mode == CP_MODE_OUTLIER)
+    return s.fast_int ? launch_composite_int_c3(s, grid, smem, stream, error)
+                      : launch_composite_f32_c3(s, grid, smem, stream, error);
+  return launch_composite_kind<3, kAnyKind>(s, grid, smem, stream, error);
 }
 
 int launch_batch_c3(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks,

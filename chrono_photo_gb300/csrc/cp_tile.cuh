@@ -571,7 +571,16 @@ DEVI void store_rows(uint8_t* out, const TileGeo& g, const uint32_t (&rows)[C][3
 }
 
 // ---- the outlier tile -----------------------------------------------------------------------
-template <int C, int NW, bool SH>
+// Kernel kinds: kAnyKind handles every stack (batches mix them); a single-stack launch takes
+// the kind of its distance arithmetic, so each kernel holds only the code it runs (smaller
+// instruction footprint, register allocation of its own).
+enum : int { kAnyKind = 0, kIntKind = 1, kF32Kind = 2 };
+template <int KIND>
+DEVI bool fast_path(const StackDev& S) {
+  return KIND == kIntKind ? true : (KIND == kF32Kind ? false : S.fast_int != 0);
+}
+
+template <int C, int NW, bool SH, int KIND>
 DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
                        Aux<C, NW>& A, uint32_t& warn_count) {
   constexpr int BP = NW <= 2 ? 4 : 2;  // byte positions per plane build (register budget)
@@ -581,7 +590,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
   uint32_t smask[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
-  const bool rel = !S.thr_abs;
+  const bool rel = KIND == kIntKind ? false : !S.thr_abs;  // the integer path is abs only
 
   // (2)+(3) planes and order statistics of word wp, BP positions per round
   {
@@ -591,17 +600,38 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     for (int kp0 = 0; kp0 < 4; kp0 += BP) {
       uint32_t P[BP][8][NW];
       build_planes<C, NW, BP, SH>(P, rd, wp, kp0, n);
-      uint32_t lo[BP], hi[BP];
-      select_multi<NW, BP>(P, smask, S.med_k, S.med_pair != 0, lo, hi);
+      uint32_t a1[BP], b1[BP], a3[BP], b3[BP];
+      if (!rel) {
+        uint32_t lo[BP], hi[BP];
+        select_multi<NW, BP>(P, smask, S.med_k, S.med_pair != 0, lo, hi);
 #pragma unroll
-      for (int k = 0; k < BP; ++k) {
-        plo |= lo[k] << (8 * (kp0 + k));
-        phi |= hi[k] << (8 * (kp0 + k));
+        for (int k = 0; k < BP; ++k) {
+          plo |= lo[k] << (8 * (kp0 + k));
+          phi |= hi[k] << (8 * (kp0 + k));
+        }
+      }
+      // rel thresholds: the median, Q1 and Q3 through one copy of the selection code (a
+      // loop rather than three inlined selections: measured faster, the instruction cache
+      // being the tighter resource)
+#pragma unroll 1
+      for (int r = 0; r < (rel ? 3 : 0); ++r) {
+        const int kr = r == 0 ? S.med_k : (r == 1 ? S.q1_k : S.q3_k);
+        const int pr = r == 0 ? S.med_pair : (r == 1 ? S.q1_pair : S.q3_pair);
+        uint32_t lo[BP], hi[BP];
+        select_multi<NW, BP>(P, smask, kr, pr != 0, lo, hi);
+#pragma unroll
+        for (int k = 0; k < BP; ++k) {
+          if (r == 0) {
+            plo |= lo[k] << (8 * (kp0 + k));
+            phi |= hi[k] << (8 * (kp0 + k));
+          }
+          a1[k] = r == 1 ? lo[k] : a1[k];
+          b1[k] = r == 1 ? hi[k] : b1[k];
+          a3[k] = lo[k];
+          b3[k] = hi[k];
+        }
       }
       if (rel) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
-        uint32_t a1[BP], b1[BP], a3[BP], b3[BP];
-        select_multi<NW, BP>(P, smask, S.q1_k, S.q1_pair != 0, a1, b1);
-        select_multi<NW, BP>(P, smask, S.q3_k, S.q3_pair != 0, a3, b3);
 #pragma unroll
         for (int k = 0; k < BP; ++k) {
           const float q1 = quantile_value(a1[k], b1[k], S.q1_pair != 0, S.q1_frac);
@@ -628,7 +658,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
   __syncthreads();
 
   // per-pixel statistics of this column
-  const bool fast = S.fast_int != 0;
+  const bool fast = fast_path<KIND>(S);
   uint32_t wbytes = 0;
 #pragma unroll
   for (int ch = 0; ch < C; ++ch)
@@ -1105,21 +1135,22 @@ DEVI void simple_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd
   store_rows<C>(S.out, g, A.out);
 }
 
-template <int C, bool SH>
+// Kinds other than kAnyKind only run outlier stacks.
+template <int C, bool SH, int KIND>
 DEVI void process_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
                        uint8_t* aux, uint32_t& warn) {
   if (S.nw == 1) {
     Aux<C, 1>& A = *reinterpret_cast<Aux<C, 1>*>(aux);
-    if (S.mode != CP_MODE_OUTLIER) simple_tile<C, 1, SH>(S, g, rd, A);
-    else outlier_tile<C, 1, SH>(S, g, rd, A, warn);
+    if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 1, SH>(S, g, rd, A);
+    else outlier_tile<C, 1, SH, KIND>(S, g, rd, A, warn);
   } else if (S.nw == 2) {
     Aux<C, 2>& A = *reinterpret_cast<Aux<C, 2>*>(aux);
-    if (S.mode != CP_MODE_OUTLIER) simple_tile<C, 2, SH>(S, g, rd, A);
-    else outlier_tile<C, 2, SH>(S, g, rd, A, warn);
+    if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 2, SH>(S, g, rd, A);
+    else outlier_tile<C, 2, SH, KIND>(S, g, rd, A, warn);
   } else {
     Aux<C, 4>& A = *reinterpret_cast<Aux<C, 4>*>(aux);
-    if (S.mode != CP_MODE_OUTLIER) simple_tile<C, 4, SH>(S, g, rd, A);
-    else outlier_tile<C, 4, SH>(S, g, rd, A, warn);
+    if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 4, SH>(S, g, rd, A);
+    else outlier_tile<C, 4, SH, KIND>(S, g, rd, A, warn);
   }
 }
 
@@ -1152,7 +1183,7 @@ DEVI void load_fbase(const StackDev& S, const SmemLayout& L) {
 
 // Stage a tile, wait for it (bounded) and process it. Returns false after a timed-out wait.
 // The exchange area sits behind the n staged rows.
-template <int C>
+template <int C, int KIND>
 DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uint32_t& phase,
                    uint32_t* error, uint32_t& warn) {
   if (threadIdx.x < 32) {
@@ -1169,17 +1200,17 @@ DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uin
   uint8_t* aux = L.buf + static_cast<size_t>(S.n) * kPitch<C>;
   if (S.shifted) {
     const Rows<C, true> rd{col, L.shifts};
-    process_tile<C, true>(S, g, rd, aux, warn);
+    process_tile<C, true, KIND>(S, g, rd, aux, warn);
   } else {
     const Rows<C, false> rd{col, L.shifts};
-    process_tile<C, false>(S, g, rd, aux, warn);
+    process_tile<C, false, KIND>(S, g, rd, aux, warn);
   }
   __syncthreads();
   return true;
 }
 
 // One stack, persistent CTAs (C warps each) striding over its tiles.
-template <int C>
+template <int C, int KIND>
 __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_constant__ StackDev S,
                                                       uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -1192,8 +1223,16 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_
   __syncthreads();
   uint32_t phase = 0, warn = 0;
   for (int t = blockIdx.x; t < S.tiles; t += gridDim.x)
-    if (!run_tile<C>(S, tile_geo(S, t), L, phase, error, warn)) return;
+    if (!run_tile<C, KIND>(S, tile_geo(S, t), L, phase, error, warn)) return;
   flush_warnings(S.warnings, warn);
+}
+
+template <int C, int KIND>
+int launch_composite_kind(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
+  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND>);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  k_composite<C, KIND><<<grid, s.threads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
+  return static_cast<int>(cudaGetLastError());
 }
 
 // Many stacks: persistent CTAs pull (stack, tile) items from a device counter.
@@ -1242,7 +1281,7 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const S
       __syncthreads();
     }
     uint32_t warn = 0;
-    if (!run_tile<C>(S, tile_geo(S, tile), L, phase, error, warn)) return;
+    if (!run_tile<C, kAnyKind>(S, tile_geo(S, tile), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
   }
 }

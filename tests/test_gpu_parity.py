@@ -102,6 +102,23 @@ def test_frame_counts(ctx, n):
 
 
 @pytest.mark.parametrize("c", [1, 3, 4])
+@pytest.mark.parametrize("n", [33, 48, 64])
+def test_rel_33_to_64_frames(ctx, n, c):
+    """Rel thresholds on 33..64 frames take the sorting-network order statistics: quartiles,
+    medians and their successors for every channel count, with weights and a subsample."""
+    rng = np.random.default_rng(300 + n * 10 + c)
+    frames = cases.random_stack(rng, n, 11, 45, c, n_spots=5)
+    compare(ctx, frames, mode="outlier", threshold="rel/2/4", outlier="extreme",
+            background="first")
+    compare(ctx, frames, mode="outlier", threshold="rel/1/3", outlier="average",
+            background="median", weights=[0.5, 1, 2, 1])
+    compare(ctx, frames, mode="outlier", threshold="rel/1.5/3", outlier="backward",
+            background="first", sample=list(range(0, n, 2)))
+    compare(ctx, frames, mode="outlier", threshold="rel/1.5/3", outlier="first",
+            background="average", sample=list(range(1, n, 3)))
+
+
+@pytest.mark.parametrize("c", [1, 3, 4])
 @pytest.mark.parametrize("shape", [(1, 1), (3, 5), (17, 29), (64, 64), (33, 300)])
 def test_shapes_channels(ctx, c, shape):
     rng = np.random.default_rng(c * 100 + shape[0])
