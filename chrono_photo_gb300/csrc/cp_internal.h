@@ -102,16 +102,11 @@ inline int smem_bytes_for(int n, int channels) {
   return kSmemHeader + n * row_pitch_host(channels) + aux_bytes(channels, nw_for(n));
 }
 
-// Per-channel-count kernel entry points (cp_kernels_c*.cu; the integer-distance and f32
-// single-stack kernels in cp_kernels_c*_int.cu / _f32.cu). Return cudaError_t values.
+// Per-channel-count kernel entry points (cp_kernels_c*.cu). Return cudaError_t values.
 #define CP_DECLARE_CH(CH)                                                                 \
   int composite_max_ctas_c##CH(int threads, int smem);                                    \
   int launch_composite_c##CH(const StackDev& s, int grid, int smem, void* stream,         \
                              uint32_t* error);                                            \
-  int launch_composite_int_c##CH(const StackDev& s, int grid, int smem, void* stream,     \
-                                 uint32_t* error);                                        \
-  int launch_composite_f32_c##CH(const StackDev& s, int grid, int smem, void* stream,     \
-                                 uint32_t* error);                                        \
   int launch_batch_c##CH(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks, \
                          int32_t total, int32_t interleave, uint32_t* counter,            \
                          uint32_t* error, int grid, int smem, void* stream);              \
@@ -121,6 +116,29 @@ CP_DECLARE_CH(1)
 CP_DECLARE_CH(3)
 CP_DECLARE_CH(4)
 #undef CP_DECLARE_CH
+
+// Single-stack outlier kernels specialised at compile time (cp_kernels_variant.cu): channels,
+// distance kind k (1 integer, 2 f32), outlier group g (0 any, 1 extreme / first / last,
+// 2 average, 3 forward / backward). RGB has one kernel per group, 1 and 4 channels one per kind.
+#define CP_DECLARE_VARIANT(CH, K, G)                                                        \
+  int launch_composite_c##CH##_k##K##_g##G(const StackDev& s, int grid, int smem,          \
+                                           void* stream, uint32_t* error);
+CP_DECLARE_VARIANT(3, 1, 1)
+CP_DECLARE_VARIANT(3, 1, 2)
+CP_DECLARE_VARIANT(3, 1, 3)
+CP_DECLARE_VARIANT(3, 2, 1)
+CP_DECLARE_VARIANT(3, 2, 2)
+CP_DECLARE_VARIANT(3, 2, 3)
+CP_DECLARE_VARIANT(1, 1, 0)
+CP_DECLARE_VARIANT(1, 2, 0)
+CP_DECLARE_VARIANT(4, 1, 0)
+CP_DECLARE_VARIANT(4, 2, 0)
+#undef CP_DECLARE_VARIANT
+// Outlier group of a stack's outlier mode.
+inline int outlier_group(int outlier) {
+  return outlier == CP_OUTLIER_AVERAGE ? 2
+         : (outlier == CP_OUTLIER_FORWARD || outlier == CP_OUTLIER_BACKWARD) ? 3 : 1;
+}
 
 // Shake search (cp_shake.cu): diffs[(f-1) * S^2 + oy*S + ox] for frames 1..n-1.
 int launch_shake(const uint8_t* const* frames_dev, int32_t n, int32_t width, int32_t height,

@@ -4,7 +4,7 @@
 namespace cp {
 
 int composite_max_ctas_c3(int threads, int smem) {
-  const void* fn = reinterpret_cast<const void*>(&k_composite<3, kAnyKind>);
+  const void* fn = reinterpret_cast<const void*>(&k_composite<3, kAnyKind, kOgAny>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess)
@@ -12,12 +12,20 @@ int composite_max_ctas_c3(int threads, int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
-// Outlier stacks go to the kernel of their distance arithmetic, the rest to the general one.
+// Outlier stacks go to the kernel of their distance arithmetic (and, for RGB, outlier group),
+// the rest to the general one.
 int launch_composite_c3(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
-  if (s.mode == CP_MODE_OUTLIER)
-    return s.fast_int ? launch_composite_int_c3(s, grid, smem, stream, error)
-                      : launch_composite_f32_c3(s, grid, smem, stream, error);
-  return launch_composite_kind<3, kAnyKind>(s, grid, smem, stream, error);
+  if (s.mode == CP_MODE_OUTLIER) {
+    const int g = outlier_group(s.outlier);
+    if (s.fast_int)
+      return g == 1 ? launch_composite_c3_k1_g1(s, grid, smem, stream, error)
+             : g == 2 ? launch_composite_c3_k1_g2(s, grid, smem, stream, error)
+                      : launch_composite_c3_k1_g3(s, grid, smem, stream, error);
+    return g == 1 ? launch_composite_c3_k2_g1(s, grid, smem, stream, error)
+           : g == 2 ? launch_composite_c3_k2_g2(s, grid, smem, stream, error)
+                    : launch_composite_c3_k2_g3(s, grid, smem, stream, error);
+  }
+  return launch_composite_kind<3, kAnyKind, kOgAny>(s, grid, smem, stream, error);
 }
 
 int launch_batch_c3(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks,

@@ -4,7 +4,7 @@
 namespace cp {
 
 int composite_max_ctas_c4(int threads, int smem) {
-  const void* fn = reinterpret_cast<const void*>(&k_composite<4, kAnyKind>);
+  const void* fn = reinterpret_cast<const void*>(&k_composite<4, kAnyKind, kOgAny>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess)
@@ -12,12 +12,13 @@ int composite_max_ctas_c4(int threads, int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
-// Outlier stacks go to the kernel of their distance arithmetic, the rest to the general one.
+// Outlier stacks go to the kernel of their distance arithmetic (and, for RGB, outlier group),
+// the rest to the general one.
 int launch_composite_c4(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
   if (s.mode == CP_MODE_OUTLIER)
-    return s.fast_int ? launch_composite_int_c4(s, grid, smem, stream, error)
-                      : launch_composite_f32_c4(s, grid, smem, stream, error);
-  return launch_composite_kind<4, kAnyKind>(s, grid, smem, stream, error);
+    return s.fast_int ? launch_composite_c4_k1_g0(s, grid, smem, stream, error)
+                      : launch_composite_c4_k2_g0(s, grid, smem, stream, error);
+  return launch_composite_kind<4, kAnyKind, kOgAny>(s, grid, smem, stream, error);
 }
 
 int launch_batch_c4(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks,

@@ -574,13 +574,24 @@ DEVI void store_rows(uint8_t* out, const TileGeo& g, const uint32_t (&rows)[C][3
 // Kernel kinds: kAnyKind handles every stack (batches mix them); a single-stack launch takes
 // the kind of its distance arithmetic, so each kernel holds only the code it runs (smaller
 // instruction footprint, register allocation of its own).
+// Likewise the outlier group (OG) fixes the epilogue: kOgSingle (extreme / first / last: one
+// sample), kOgAverage, kOgBlend (forward / backward), or kOgAny.
 enum : int { kAnyKind = 0, kIntKind = 1, kF32Kind = 2 };
+enum : int { kOgAny = 0, kOgSingle = 1, kOgAverage = 2, kOgBlend = 3 };
 template <int KIND>
 DEVI bool fast_path(const StackDev& S) {
   return KIND == kIntKind ? true : (KIND == kF32Kind ? false : S.fast_int != 0);
 }
+template <int OG>
+DEVI bool og_is(const StackDev& S, int og) {
+  if (OG != kOgAny) return OG == og;
+  const int m = S.outlier;
+  if (og == kOgAverage) return m == CP_OUTLIER_AVERAGE;
+  if (og == kOgBlend) return m == CP_OUTLIER_FORWARD || m == CP_OUTLIER_BACKWARD;
+  return m == CP_OUTLIER_EXTREME || m == CP_OUTLIER_FIRST || m == CP_OUTLIER_LAST;
+}
 
-template <int C, int NW, bool SH, int KIND>
+template <int C, int NW, bool SH, int KIND, int OG>
 DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
                        Aux<C, NW>& A, uint32_t& warn_count) {
   constexpr int BP = NW <= 2 ? 4 : 2;  // byte positions per plane build (register budget)
@@ -962,13 +973,14 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     float blend = 0.0f;
     int chosen = -1;
     uint32_t mask = 0;
-    const bool multi = nout > 1 && (S.outlier == CP_OUTLIER_AVERAGE ||
-                                    S.outlier == CP_OUTLIER_FORWARD ||
-                                    S.outlier == CP_OUTLIER_BACKWARD);
+    const bool single_group = og_is<OG>(S, kOgSingle);
+    const bool blend_group = og_is<OG>(S, kOgBlend);
+    const bool extreme = single_group && S.outlier == CP_OUTLIER_EXTREME;
+    const bool multi = nout > 1 && !single_group;
     if (!multi) {
       int si;
       float dsq;
-      if (S.outlier == CP_OUTLIER_EXTREME) {
+      if (extreme) {
         si = pimax;
         if (fast) {
           const int32_t dm = pdmax_i;
@@ -977,17 +989,18 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
           dsq = pdmax_f;
         }
       } else {
-        si = S.outlier == CP_OUTLIER_LAST ? last_set<NW>(pb) : first_set<NW>(pb);
+        // the multi-outlier groups come here with at most one outlier: first == last
+        si = (single_group && S.outlier == CP_OUTLIER_LAST) ? last_set<NW>(pb) : first_set<NW>(pb);
         si = si < 0 ? 0 : si;
       }
       const uint32_t sample = load_pixel<C, SH>(rd, si, p);
-      if (S.outlier != CP_OUTLIER_EXTREME) dsq = dsq_px(sample);
+      if (!extreme) dsq = dsq_px(sample);
       blend = nout == 0 ? 0.0f : __fmul_rn(S.fade[si], blend_value(S, __fsqrt_rn(dsq)));
       pix = blend_into_u8<C>(pix, sample, blend);
       mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
       chosen = nout == 0 ? -1 : si;
     } else {
-      if (S.outlier == CP_OUTLIER_FORWARD || S.outlier == CP_OUTLIER_BACKWARD) {
+      if (blend_group) {
         float pf[C];
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((pix >> (8 * ch)) & 0xFFu);
@@ -1136,21 +1149,21 @@ DEVI void simple_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd
 }
 
 // Kinds other than kAnyKind only run outlier stacks.
-template <int C, bool SH, int KIND>
+template <int C, bool SH, int KIND, int OG>
 DEVI void process_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
                        uint8_t* aux, uint32_t& warn) {
   if (S.nw == 1) {
     Aux<C, 1>& A = *reinterpret_cast<Aux<C, 1>*>(aux);
     if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 1, SH>(S, g, rd, A);
-    else outlier_tile<C, 1, SH, KIND>(S, g, rd, A, warn);
+    else outlier_tile<C, 1, SH, KIND, OG>(S, g, rd, A, warn);
   } else if (S.nw == 2) {
     Aux<C, 2>& A = *reinterpret_cast<Aux<C, 2>*>(aux);
     if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 2, SH>(S, g, rd, A);
-    else outlier_tile<C, 2, SH, KIND>(S, g, rd, A, warn);
+    else outlier_tile<C, 2, SH, KIND, OG>(S, g, rd, A, warn);
   } else {
     Aux<C, 4>& A = *reinterpret_cast<Aux<C, 4>*>(aux);
     if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 4, SH>(S, g, rd, A);
-    else outlier_tile<C, 4, SH, KIND>(S, g, rd, A, warn);
+    else outlier_tile<C, 4, SH, KIND, OG>(S, g, rd, A, warn);
   }
 }
 
@@ -1183,7 +1196,7 @@ DEVI void load_fbase(const StackDev& S, const SmemLayout& L) {
 
 // Stage a tile, wait for it (bounded) and process it. Returns false after a timed-out wait.
 // The exchange area sits behind the n staged rows.
-template <int C, int KIND>
+template <int C, int KIND, int OG>
 DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uint32_t& phase,
                    uint32_t* error, uint32_t& warn) {
   if (threadIdx.x < 32) {
@@ -1200,17 +1213,17 @@ DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uin
   uint8_t* aux = L.buf + static_cast<size_t>(S.n) * kPitch<C>;
   if (S.shifted) {
     const Rows<C, true> rd{col, L.shifts};
-    process_tile<C, true, KIND>(S, g, rd, aux, warn);
+    process_tile<C, true, KIND, OG>(S, g, rd, aux, warn);
   } else {
     const Rows<C, false> rd{col, L.shifts};
-    process_tile<C, false, KIND>(S, g, rd, aux, warn);
+    process_tile<C, false, KIND, OG>(S, g, rd, aux, warn);
   }
   __syncthreads();
   return true;
 }
 
 // One stack, persistent CTAs (C warps each) striding over its tiles.
-template <int C, int KIND>
+template <int C, int KIND, int OG>
 __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_constant__ StackDev S,
                                                       uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -1223,15 +1236,15 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_
   __syncthreads();
   uint32_t phase = 0, warn = 0;
   for (int t = blockIdx.x; t < S.tiles; t += gridDim.x)
-    if (!run_tile<C, KIND>(S, tile_geo(S, t), L, phase, error, warn)) return;
+    if (!run_tile<C, KIND, OG>(S, tile_geo(S, t), L, phase, error, warn)) return;
   flush_warnings(S.warnings, warn);
 }
 
-template <int C, int KIND>
+template <int C, int KIND, int OG>
 int launch_composite_kind(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
-  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND>);
+  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND, OG>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_composite<C, KIND><<<grid, s.threads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
+  k_composite<C, KIND, OG><<<grid, s.threads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -1281,7 +1294,7 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const S
       __syncthreads();
     }
     uint32_t warn = 0;
-    if (!run_tile<C, kAnyKind>(S, tile_geo(S, tile), L, phase, error, warn)) return;
+    if (!run_tile<C, kAnyKind, kOgAny>(S, tile_geo(S, tile), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
   }
 }
