@@ -283,13 +283,14 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
         ctx->occupancy[std::make_pair(key, 0)] = per_sm;
       }
     }
-    const int items = (d.px_end - d.px_begin) / 16 + (d.px_end - d.px_begin) % 16;
-    const int grid = std::max(1, std::min((items + 255) / 256, per_sm * ctx->sm_count));
+    const int chunk = simple_stream_chunk_px_c3();  // the same for every channel count
+    const int chunks = (d.px_end - d.px_begin + chunk - 1) / chunk;
+    const int grid = std::max(1, std::min(chunks, per_sm * ctx->sm_count));
     int rc;
     switch (d.channels) {
-      case 1: rc = launch_simple_stream_c1(d, fast, grid, stream); break;
-      case 3: rc = launch_simple_stream_c3(d, fast, grid, stream); break;
-      default: rc = launch_simple_stream_c4(d, fast, grid, stream); break;
+      case 1: rc = launch_simple_stream_c1(d, fast, grid, stream, ctx->d_error); break;
+      case 3: rc = launch_simple_stream_c3(d, fast, grid, stream, ctx->d_error); break;
+      default: rc = launch_simple_stream_c4(d, fast, grid, stream, ctx->d_error); break;
     }
     return cuda_status(ctx, static_cast<cudaError_t>(rc), "simple launch");
   }

@@ -111,7 +111,9 @@ inline int smem_bytes_for(int n, int channels) {
                          int32_t total, int32_t interleave, uint32_t* counter,            \
                          uint32_t* error, int grid, int smem, void* stream);              \
   int simple_stream_max_ctas_c##CH(bool fast);                                            \
-  int launch_simple_stream_c##CH(const StackDev& s, bool fast, int grid, void* stream);
+  int simple_stream_chunk_px_c##CH();                                                     \
+  int launch_simple_stream_c##CH(const StackDev& s, bool fast, int grid, void* stream,    \
+                                 uint32_t* error);
 CP_DECLARE_CH(1)
 CP_DECLARE_CH(3)
 CP_DECLARE_CH(4)

@@ -35,15 +35,20 @@ int simple_stream_max_ctas_c1(bool fast) {
   const void* fn = fast ? reinterpret_cast<const void*>(&k_simple_stream<1, true>)
                         : reinterpret_cast<const void*>(&k_simple_stream<1, false>);
   int blocks = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 256, 0) != cudaSuccess) return 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kStreamThreads, kStreamSmem<1>) !=
+      cudaSuccess)
+    return 1;
   return blocks < 1 ? 1 : blocks;
 }
 
-int launch_simple_stream_c1(const StackDev& s, bool fast, int grid, void* stream) {
+int simple_stream_chunk_px_c1() { return kStreamChunkPx; }
+
+int launch_simple_stream_c1(const StackDev& s, bool fast, int grid, void* stream, uint32_t* error) {
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (fast)
-    k_simple_stream<1, true><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(s);
+    k_simple_stream<1, true><<<grid, kStreamThreads, kStreamSmem<1>, st>>>(s, error);
   else
-    k_simple_stream<1, false><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(s);
+    k_simple_stream<1, false><<<grid, kStreamThreads, kStreamSmem<1>, st>>>(s, error);
   return static_cast<int>(cudaGetLastError());
 }
 

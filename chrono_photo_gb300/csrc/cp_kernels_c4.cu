@@ -35,15 +35,20 @@ int simple_stream_max_ctas_c4(bool fast) {
   const void* fn = fast ? reinterpret_cast<const void*>(&k_simple_stream<4, true>)
                         : reinterpret_cast<const void*>(&k_simple_stream<4, false>);
   int blocks = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 256, 0) != cudaSuccess) return 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kStreamThreads, kStreamSmem<4>) !=
+      cudaSuccess)
+    return 1;
   return blocks < 1 ? 1 : blocks;
 }
 
-int launch_simple_stream_c4(const StackDev& s, bool fast, int grid, void* stream) {
+int simple_stream_chunk_px_c4() { return kStreamChunkPx; }
+
+int launch_simple_stream_c4(const StackDev& s, bool fast, int grid, void* stream, uint32_t* error) {
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (fast)
-    k_simple_stream<4, true><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(s);
+    k_simple_stream<4, true><<<grid, kStreamThreads, kStreamSmem<4>, st>>>(s, error);
   else
-    k_simple_stream<4, false><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(s);
+    k_simple_stream<4, false><<<grid, kStreamThreads, kStreamSmem<4>, st>>>(s, error);
   return static_cast<int>(cudaGetLastError());
 }
 

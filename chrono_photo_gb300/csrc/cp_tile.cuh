@@ -1299,130 +1299,156 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const S
   }
 }
 
-// darker/lighter streaming over an aligned, uncropped stack (no shared-memory staging): each
-// thread owns 16 pixels, i.e. C 16-byte words of every frame, and folds its frames in order
-// with 128-bit loads, four frames in flight. FAST: weights 0/1 and every fade >= 1, where the
-// f32 sum of src/simple.rs:103-106 is an exact integer and a new extreme copies the pixel.
+// darker/lighter streaming over an aligned, uncropped stack: a CTA of 128 threads owns chunks
+// of 2048 pixels (16 per thread) and pulls the chunk's row of every frame through a ring of
+// kStreamStages shared-memory stages with one cp.async.bulk each (TMA engine; thread 0 issues
+// stage s again as soon as all threads have folded it), so several frame rows per CTA are in
+// flight at all times. Each thread folds its 16 pixels frame by frame in order. FAST: weights
+// 0/1 and every fade >= 1, where the f32 sum of src/simple.rs:103-106 is an exact integer and
+// a new extreme copies the pixel.
+constexpr int kStreamThreads = 128;
+constexpr int kStreamPx = 16;  // pixels per thread
+constexpr int kStreamStages = 4;
+constexpr int kStreamChunkPx = kStreamThreads * kStreamPx;
+template <int C>
+constexpr int kStreamStageBytes = kStreamChunkPx * C;
+
 template <int C, bool FAST>
-__global__ void __launch_bounds__(256) k_simple_stream(const __grid_constant__ StackDev S) {
+__global__ void __launch_bounds__(kStreamThreads, 8)
+    k_simple_stream(const __grid_constant__ StackDev S, uint32_t* error) {
   constexpr int NWD = 4 * C;  // 32-bit words per thread per frame
+  extern __shared__ __align__(128) uint8_t smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint8_t* stage = smem + 128;
   const bool darker = S.mode == CP_MODE_DARKER;
-  const int groups = (S.px_end - S.px_begin) / 16;
-  const int tail = (S.px_end - S.px_begin) - 16 * groups;
   const int n = S.n;
+  const int P = S.px_end - S.px_begin;
+  const int chunks = (P + kStreamChunkPx - 1) / kStreamChunkPx;
+  const int mine = static_cast<int>(blockIdx.x) < chunks
+                       ? (chunks - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
+                       : 0;
+  const int items = mine * n;  // (chunk, frame) in chunk-major order
+  if (items == 0) return;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int st = 0; st < kStreamStages; ++st) mbar_init(&full[st], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto chunk_px0 = [&](int i) {
+    return S.px_begin + (static_cast<int>(blockIdx.x) + (i / n) * static_cast<int>(gridDim.x)) *
+                            kStreamChunkPx;
+  };
+  auto issue = [&](int i) {  // thread 0: item i into stage i % kStreamStages
+    const int px0 = chunk_px0(i);
+    const int npx = min(kStreamChunkPx, S.px_end - px0);
+    const uint32_t bytes = (static_cast<uint32_t>(npx * C) + 15u) & ~15u;
+    uint64_t* bar = &full[i % kStreamStages];
+    mbar_expect_tx(bar, bytes);
+    bulk_g2s(stage + (i % kStreamStages) * kStreamStageBytes<C>,
+             S.frames[i % n] + static_cast<size_t>(px0) * C, bytes, bar);
+  };
+  if (threadIdx.x == 0)
+    for (int i = 0; i < min(kStreamStages, items); ++i) issue(i);
   uint32_t wbytes = 0;
 #pragma unroll
   for (int ch = 0; ch < C; ++ch)
     if ((S.wmask >> ch) & 1u) wbytes |= 0xFFu << (8 * ch);
-  const int stride = gridDim.x * blockDim.x;
-  for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < groups + tail; gi += stride) {
-    if (gi >= groups) {  // tail pixels one by one
-      const size_t o = static_cast<size_t>(S.px_begin + 16 * groups + (gi - groups)) * C;
-      float ext = darker ? FLT_MAX : -FLT_MAX;
-      uint32_t out = 0;
-      for (int f = 0; f < n; ++f) {
-        uint32_t px = 0;
+  int32_t exti[kStreamPx];
+  float extf[kStreamPx];
+  uint32_t outw[kStreamPx];
+  for (int i = 0; i < items; ++i) {
+    const int f = i % n, st = i % kStreamStages;
+    if (f == 0) {
 #pragma unroll
-        for (int ch = 0; ch < C; ++ch) px |= static_cast<uint32_t>(S.frames[f][o + ch]) << (8 * ch);
-        float value = 0.0f;
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch)
-          value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
-        const bool up = darker ? (value < ext) : (value > ext);
-        ext = up ? value : ext;
-        const float fade = S.fade[f];
-        if (up && fade > 0.0f) out = fade >= 1.0f ? px : blend_into_u8<C>(out, px, fade);
+      for (int p = 0; p < kStreamPx; ++p) {
+        exti[p] = darker ? 0x7FFFFFFF : -1;
+        extf[p] = darker ? FLT_MAX : -FLT_MAX;
+        outw[p] = 0u;
       }
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) S.out[o + ch] = static_cast<uint8_t>(out >> (8 * ch));
-      continue;
     }
-    const size_t off = static_cast<size_t>(S.px_begin + 16 * gi) * C;
-    int32_t exti[16];
-    float extf[16];
-    uint32_t outw[16];
-#pragma unroll
-    for (int p = 0; p < 16; ++p) {
-      exti[p] = darker ? 0x7FFFFFFF : -1;
-      extf[p] = darker ? FLT_MAX : -FLT_MAX;
-      outw[p] = 0u;
+    if (!mbar_wait(&full[st], static_cast<uint32_t>(i / kStreamStages) & 1u)) {
+      if (error) atomicOr(error, 1u);
+      // the other stages' copies in flight complete (bounded) before the CTA leaves
+      for (int j = i + 1; j < min(i + kStreamStages, items); ++j)
+        mbar_wait(&full[j % kStreamStages], static_cast<uint32_t>(j / kStreamStages) & 1u);
+      return;
     }
-    auto fold = [&](const uint32_t (&wv)[NWD], int f) {
+    uint32_t wv[NWD];
+    const uint4* src = reinterpret_cast<const uint4*>(stage + st * kStreamStageBytes<C> +
+                                                      threadIdx.x * (kStreamPx * C));
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        uint32_t sub[C];
+    for (int q = 0; q < C; ++q) {
+      const uint4 v = src[q];
+      wv[4 * q] = v.x;
+      wv[4 * q + 1] = v.y;
+      wv[4 * q + 2] = v.z;
+      wv[4 * q + 3] = v.w;
+    }
 #pragma unroll
-        for (int i = 0; i < C; ++i) sub[i] = wv[q * C + i];
+    for (int q = 0; q < 4; ++q) {
+      uint32_t sub[C];
 #pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          const int pp = q * 4 + p;
-          const uint32_t px = pixel_word<C>(sub, p);
-          if constexpr (FAST) {
-            const int32_t v = static_cast<int32_t>(__dp4a(px & wbytes, 0x01010101u, 0u));
-            const bool up = darker ? v < exti[pp] : v > exti[pp];
-            exti[pp] = up ? v : exti[pp];
-            outw[pp] = up ? px : outw[pp];
-          } else {
-            float value = 0.0f;
+      for (int k = 0; k < C; ++k) sub[k] = wv[q * C + k];
 #pragma unroll
-            for (int ch = 0; ch < C; ++ch)
-              value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
-            const bool up = darker ? (value < extf[pp]) : (value > extf[pp]);
-            extf[pp] = up ? value : extf[pp];
-            const float fade = S.fade[f];
-            if (up && fade > 0.0f)
-              outw[pp] = fade >= 1.0f ? px : blend_into_u8<C>(outw[pp], px, fade);
+      for (int p = 0; p < 4; ++p) {
+        const int pp = q * 4 + p;
+        const uint32_t px = pixel_word<C>(sub, p);
+        if constexpr (FAST) {
+          const int32_t v = static_cast<int32_t>(__dp4a(px & wbytes, 0x01010101u, 0u));
+          const bool up = darker ? v < exti[pp] : v > exti[pp];
+          exti[pp] = up ? v : exti[pp];
+          outw[pp] = up ? px : outw[pp];
+        } else {
+          float value = 0.0f;
+#pragma unroll
+          for (int ch = 0; ch < C; ++ch)
+            value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
+          const bool up = darker ? (value < extf[pp]) : (value > extf[pp]);
+          extf[pp] = up ? value : extf[pp];
+          const float fade = S.fade[f];
+          if (up && fade > 0.0f)
+            outw[pp] = fade >= 1.0f ? px : blend_into_u8<C>(outw[pp], px, fade);
+        }
+      }
+    }
+    if (f == n - 1) {  // the chunk's 16 pixels of this thread: C 16-byte words
+      const int px = chunk_px0(i) + static_cast<int>(threadIdx.x) * kStreamPx;
+      uint32_t ow[NWD];
+#pragma unroll
+      for (int k = 0; k < NWD; ++k) ow[k] = 0u;
+#pragma unroll
+      for (int pp = 0; pp < kStreamPx; ++pp)
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+          const int bb = pp * C + ch;
+          ow[bb / 4] |= ((outw[pp] >> (8 * ch)) & 0xFFu) << (8 * (bb % 4));
+        }
+      uint8_t* dst = S.out + static_cast<size_t>(px) * C;
+      if (px + kStreamPx <= S.px_end) {
+#pragma unroll
+        for (int q = 0; q < C; ++q)
+          reinterpret_cast<uint4*>(dst)[q] =
+              make_uint4(ow[4 * q], ow[4 * q + 1], ow[4 * q + 2], ow[4 * q + 3]);
+      } else if (px < S.px_end) {
+        const int valid = S.px_end - px;
+#pragma unroll
+        for (int pp = 0; pp < kStreamPx; ++pp)
+          if (pp < valid) {
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) dst[pp * C + ch] = static_cast<uint8_t>(outw[pp] >> (8 * ch));
           }
-        }
       }
-    };
-    int f = 0;
-    for (; f + 4 <= n; f += 4) {
-      uint32_t wv[4][NWD];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint4* src = reinterpret_cast<const uint4*>(S.frames[f + j] + off);
-#pragma unroll
-        for (int i = 0; i < C; ++i) {
-          const uint4 v = __ldcs(src + i);  // streamed once: evict first
-          wv[j][4 * i] = v.x;
-          wv[j][4 * i + 1] = v.y;
-          wv[j][4 * i + 2] = v.z;
-          wv[j][4 * i + 3] = v.w;
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) fold(wv[j], f + j);
     }
-    for (; f < n; ++f) {
-      uint32_t wv[NWD];
-      const uint4* src = reinterpret_cast<const uint4*>(S.frames[f] + off);
-#pragma unroll
-      for (int i = 0; i < C; ++i) {
-        const uint4 v = __ldcs(src + i);
-        wv[4 * i] = v.x;
-        wv[4 * i + 1] = v.y;
-        wv[4 * i + 2] = v.z;
-        wv[4 * i + 3] = v.w;
-      }
-      fold(wv, f);
+    __syncthreads();  // stage st folded by every thread
+    if (threadIdx.x == 0 && i + kStreamStages < items) {
+      fence_proxy_async();
+      issue(i + kStreamStages);
     }
-    // 16 pixels = C 16-byte words
-    uint32_t ow[NWD];
-#pragma unroll
-    for (int i = 0; i < NWD; ++i) ow[i] = 0u;
-#pragma unroll
-    for (int pp = 0; pp < 16; ++pp)
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) {
-        const int b = pp * C + ch;
-        ow[b / 4] |= ((outw[pp] >> (8 * ch)) & 0xFFu) << (8 * (b % 4));
-      }
-    uint4* dst = reinterpret_cast<uint4*>(S.out + off);
-#pragma unroll
-    for (int i = 0; i < C; ++i) dst[i] = make_uint4(ow[4 * i], ow[4 * i + 1], ow[4 * i + 2], ow[4 * i + 3]);
   }
 }
+template <int C>
+constexpr int kStreamSmem = 128 + kStreamStages * kStreamStageBytes<C>;
 
 }  // namespace
 }  // namespace cp
