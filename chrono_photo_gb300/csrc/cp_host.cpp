@@ -300,7 +300,9 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
     return CP_ERR_ARG;
   }
   int per_sm = 1, rc = 0;
-  const auto key = std::make_pair(d.channels, smem);
+  // occupancy of the kernel this stack launches with, cached per (variant, channels, smem)
+  const auto key = std::make_pair(
+      2000 + 16 * d.channels + single_variant(d.mode, d.fast_int, d.outlier), smem);
   {
     std::lock_guard<std::mutex> lk(ctx->mu);
     auto it = ctx->occupancy.find(key);
@@ -308,9 +310,9 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
       per_sm = it->second;
     } else {
       switch (d.channels) {
-        case 1: per_sm = composite_max_ctas_c1(d.threads, smem); break;
-        case 3: per_sm = composite_max_ctas_c3(d.threads, smem); break;
-        default: per_sm = composite_max_ctas_c4(d.threads, smem); break;
+        case 1: per_sm = single_max_ctas_c1(d, smem); break;
+        case 3: per_sm = single_max_ctas_c3(d, smem); break;
+        default: per_sm = single_max_ctas_c4(d, smem); break;
       }
       ctx->occupancy[key] = per_sm;
     }

@@ -52,7 +52,7 @@ struct cp_ctx {
   std::mutex call_mu; // serialises the host-staged entry points (shared staging buffers)
   std::string last_error;
   std::map<void*, uint64_t> allocs;
-  std::map<std::pair<int, int>, int> occupancy;  // (channels, smem) -> CTAs per SM
+  std::map<std::pair<int, int>, int> occupancy;  // (kernel key, smem) -> CTAs per SM
   uint32_t* d_error = nullptr;               // device error flags of bounded waits
   unsigned long long* d_warn = nullptr;      // device warning counter (host-staged calls)
   // host-staged composite: device copies of the frames and outputs, pinned staging

@@ -104,7 +104,8 @@ inline int smem_bytes_for(int n, int channels) {
 
 // Per-channel-count kernel entry points (cp_kernels_c*.cu). Return cudaError_t values.
 #define CP_DECLARE_CH(CH)                                                                 \
-  int composite_max_ctas_c##CH(int threads, int smem);                                    \
+  int composite_max_ctas_c##CH(int threads, int smem); /* the batch (any-stack) kernel */  \
+  int single_max_ctas_c##CH(const StackDev& s, int smem); /* the kernel s launches with */ \
   int launch_composite_c##CH(const StackDev& s, int grid, int smem, void* stream,         \
                              uint32_t* error);                                            \
   int launch_batch_c##CH(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks, \
@@ -124,7 +125,8 @@ CP_DECLARE_CH(4)
 // 2 average, 3 forward / backward). RGB has one kernel per group, 1 and 4 channels one per kind.
 #define CP_DECLARE_VARIANT(CH, K, G)                                                        \
   int launch_composite_c##CH##_k##K##_g##G(const StackDev& s, int grid, int smem,          \
-                                           void* stream, uint32_t* error);
+                                           void* stream, uint32_t* error);                 \
+  int max_ctas_c##CH##_k##K##_g##G(int threads, int smem);
 CP_DECLARE_VARIANT(3, 1, 1)
 CP_DECLARE_VARIANT(3, 1, 2)
 CP_DECLARE_VARIANT(3, 1, 3)
@@ -140,6 +142,10 @@ CP_DECLARE_VARIANT(4, 2, 0)
 inline int outlier_group(int outlier) {
   return outlier == CP_OUTLIER_AVERAGE ? 2
          : (outlier == CP_OUTLIER_FORWARD || outlier == CP_OUTLIER_BACKWARD) ? 3 : 1;
+}
+// Which single-stack kernel a stack launches with (an occupancy cache key).
+inline int single_variant(int mode, uint32_t fast_int, int outlier) {
+  return mode != CP_MODE_OUTLIER ? 0 : (fast_int ? 1 : 2) * 4 + outlier_group(outlier);
 }
 
 // Shake search (cp_shake.cu): diffs[(f-1) * S^2 + oy*S + ox] for frames 1..n-1.

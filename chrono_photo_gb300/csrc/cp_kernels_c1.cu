@@ -12,6 +12,12 @@ int composite_max_ctas_c1(int threads, int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
+int single_max_ctas_c1(const StackDev& s, int smem) {
+  if (s.mode == CP_MODE_OUTLIER)
+    return s.fast_int ? max_ctas_c1_k1_g0(s.threads, smem) : max_ctas_c1_k2_g0(s.threads, smem);
+  return max_ctas_kind<1, kAnyKind, kOgAny>(s.threads, smem);
+}
+
 // Outlier stacks go to the kernel of their distance arithmetic (and, for RGB, outlier group),
 // the rest to the general one.
 int launch_composite_c1(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {

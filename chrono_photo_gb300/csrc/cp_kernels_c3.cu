@@ -12,6 +12,18 @@ int composite_max_ctas_c3(int threads, int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
+int single_max_ctas_c3(const StackDev& s, int smem) {
+  if (s.mode == CP_MODE_OUTLIER) {
+    const int g = outlier_group(s.outlier);
+    if (s.fast_int)
+      return g == 1 ? max_ctas_c3_k1_g1(s.threads, smem)
+             : g == 2 ? max_ctas_c3_k1_g2(s.threads, smem) : max_ctas_c3_k1_g3(s.threads, smem);
+    return g == 1 ? max_ctas_c3_k2_g1(s.threads, smem)
+           : g == 2 ? max_ctas_c3_k2_g2(s.threads, smem) : max_ctas_c3_k2_g3(s.threads, smem);
+  }
+  return max_ctas_kind<3, kAnyKind, kOgAny>(s.threads, smem);
+}
+
 // Outlier stacks go to the kernel of their distance arithmetic (and, for RGB, outlier group),
 // the rest to the general one.
 int launch_composite_c3(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {

@@ -19,4 +19,8 @@ int CP_CAT(launch_composite_c, CP_CH, _k, CP_KIND, _g, CP_OG)(const StackDev& s,
   return launch_composite_kind<CP_CH, CP_KIND, CP_OG>(s, grid, smem, stream, error);
 }
 
+int CP_CAT(max_ctas_c, CP_CH, _k, CP_KIND, _g, CP_OG)(int threads, int smem) {
+  return max_ctas_kind<CP_CH, CP_KIND, CP_OG>(threads, smem);
+}
+
 }  // namespace cp

@@ -1241,6 +1241,16 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_
 }
 
 template <int C, int KIND, int OG>
+int max_ctas_kind(int threads, int smem) {
+  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND, OG>);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess)
+    return 1;
+  return blocks < 1 ? 1 : blocks;
+}
+
+template <int C, int KIND, int OG>
 int launch_composite_kind(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
   const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND, OG>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
