@@ -25,9 +25,10 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"
 CU_SOURCES = ["cp_kernels_c3.cu", "cp_kernels_c4.cu", "cp_kernels_c1.cu", "cp_shake.cu",
               "cp_static.cu"]
 # cp_kernels_variant.cu compiled once per specialised single-stack outlier kernel:
-# (channels, distance kind, outlier group), see cp_internal.h
-KERNEL_VARIANTS = [(3, 1, 1), (3, 1, 2), (3, 1, 3), (3, 2, 1), (3, 2, 2), (3, 2, 3),
-                   (1, 1, 0), (1, 2, 0), (4, 1, 0), (4, 2, 0)]
+# (channels, distance kind, outlier group, background), the CP_VARIANTS list of cp_internal.h
+KERNEL_VARIANTS = [(3, k, g, b) for k in (1, 2) for b in (1, 0) for g in (1, 2, 3)] + \
+    [(3, 3, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0), (1, 3, 0, 0), (4, 1, 0, 0), (4, 2, 0, 0),
+     (4, 3, 0, 0)]
 CPP_SOURCES = ["cp_host.cpp", "cp_stage.cpp", "cp_batch.cpp", "cp_shake_host.cpp",
                "cp_server.cpp"]
 HEADERS = ["cp_internal.h", "cp_host_internal.h", "cp_tile.cuh"]
@@ -71,12 +72,13 @@ def build(verbose=False, jobs=None):
         if _stale(o, [s] + hdrs):
             steps.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
     vsrc = os.path.join(CSRC, "cp_kernels_variant.cu")
-    for ch, kind, og in KERNEL_VARIANTS:
-        o = os.path.join(OBJ_DIR, "cp_kernels_c%d_k%d_g%d.o" % (ch, kind, og))
+    for ch, kind, og, bg in KERNEL_VARIANTS:
+        o = os.path.join(OBJ_DIR, "cp_kernels_c%d_k%d_g%d_b%d.o" % (ch, kind, og, bg))
         objs.append(o)
         if _stale(o, [vsrc] + hdrs):
-            steps.append([nvcc] + ARCH + NVCC_FLAGS + ["-DCP_CH=%d" % ch, "-DCP_KIND=%d" % kind,
-                                                      "-DCP_OG=%d" % og, "-c", vsrc, "-o", o])
+            steps.append([nvcc] + ARCH + NVCC_FLAGS + [
+                "-DCP_CH=%d" % ch, "-DCP_KIND=%d" % kind, "-DCP_OG=%d" % og, "-DCP_BG=%d" % bg,
+                "-c", vsrc, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ_DIR, src + ".o")

@@ -300,28 +300,53 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
     return CP_ERR_ARG;
   }
   int per_sm = 1, rc = 0;
+  const bool outlier = d.mode == CP_MODE_OUTLIER;
+  int k = 0, g = 0, b = 0;
+  if (outlier) outlier_variant(d, &k, &g, &b);
   // occupancy of the kernel this stack launches with, cached per (variant, channels, smem)
-  const auto key = std::make_pair(
-      2000 + 16 * d.channels + single_variant(d.mode, d.fast_int, d.outlier), smem);
+  const auto key = std::make_pair(2000 + 64 * d.channels + single_variant(d), smem);
   {
     std::lock_guard<std::mutex> lk(ctx->mu);
     auto it = ctx->occupancy.find(key);
     if (it != ctx->occupancy.end()) {
       per_sm = it->second;
     } else {
-      switch (d.channels) {
-        case 1: per_sm = single_max_ctas_c1(d, smem); break;
-        case 3: per_sm = single_max_ctas_c3(d, smem); break;
-        default: per_sm = single_max_ctas_c4(d, smem); break;
+      per_sm = 0;
+      if (outlier) {
+#define CP_VARIANT_OCC(CH, K, G, B)                                      \
+  if (d.channels == CH && k == K && g == G && b == B)                  \
+    per_sm = max_ctas_c##CH##_k##K##_g##G##_b##B(d.threads, smem);
+        CP_VARIANTS(CP_VARIANT_OCC)
+#undef CP_VARIANT_OCC
+      } else {
+        switch (d.channels) {
+          case 1: per_sm = composite_max_ctas_c1(d.threads, smem); break;
+          case 3: per_sm = composite_max_ctas_c3(d.threads, smem); break;
+          default: per_sm = composite_max_ctas_c4(d.threads, smem); break;
+        }
       }
+      if (per_sm < 1) per_sm = 1;
       ctx->occupancy[key] = per_sm;
     }
   }
   const int grid = std::max(1, std::min(d.tiles, per_sm * ctx->sm_count));
-  switch (d.channels) {
-    case 1: rc = launch_composite_c1(d, grid, smem, stream, ctx->d_error); break;
-    case 3: rc = launch_composite_c3(d, grid, smem, stream, ctx->d_error); break;
-    default: rc = launch_composite_c4(d, grid, smem, stream, ctx->d_error); break;
+  rc = -1;
+  if (outlier) {
+#define CP_VARIANT_LAUNCH(CH, K, G, B)                                             \
+  if (d.channels == CH && k == K && g == G && b == B)                            \
+    rc = launch_composite_c##CH##_k##K##_g##G##_b##B(d, grid, smem, stream, ctx->d_error);
+    CP_VARIANTS(CP_VARIANT_LAUNCH)
+#undef CP_VARIANT_LAUNCH
+    if (rc < 0) {
+      ctx_error(ctx, "no kernel for %d channels, variant %d/%d/%d", d.channels, k, g, b);
+      return CP_ERR_ARG;
+    }
+  } else {
+    switch (d.channels) {
+      case 1: rc = launch_composite_c1(d, grid, smem, stream, ctx->d_error); break;
+      case 3: rc = launch_composite_c3(d, grid, smem, stream, ctx->d_error); break;
+      default: rc = launch_composite_c4(d, grid, smem, stream, ctx->d_error); break;
+    }
   }
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "composite launch");
 }

@@ -104,8 +104,7 @@ inline int smem_bytes_for(int n, int channels) {
 
 // Per-channel-count kernel entry points (cp_kernels_c*.cu). Return cudaError_t values.
 #define CP_DECLARE_CH(CH)                                                                 \
-  int composite_max_ctas_c##CH(int threads, int smem); /* the batch (any-stack) kernel */  \
-  int single_max_ctas_c##CH(const StackDev& s, int smem); /* the kernel s launches with */ \
+  int composite_max_ctas_c##CH(int threads, int smem); /* the general (any-stack) kernel */\
   int launch_composite_c##CH(const StackDev& s, int grid, int smem, void* stream,         \
                              uint32_t* error);                                            \
   int launch_batch_c##CH(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks, \
@@ -120,32 +119,40 @@ CP_DECLARE_CH(3)
 CP_DECLARE_CH(4)
 #undef CP_DECLARE_CH
 
-// Single-stack outlier kernels specialised at compile time (cp_kernels_variant.cu): channels,
-// distance kind k (1 integer, 2 f32), outlier group g (0 any, 1 extreme / first / last,
-// 2 average, 3 forward / backward). RGB has one kernel per group, 1 and 4 channels one per kind.
-#define CP_DECLARE_VARIANT(CH, K, G)                                                        \
-  int launch_composite_c##CH##_k##K##_g##G(const StackDev& s, int grid, int smem,          \
-                                           void* stream, uint32_t* error);                 \
-  int max_ctas_c##CH##_k##K##_g##G(int threads, int smem);
-CP_DECLARE_VARIANT(3, 1, 1)
-CP_DECLARE_VARIANT(3, 1, 2)
-CP_DECLARE_VARIANT(3, 1, 3)
-CP_DECLARE_VARIANT(3, 2, 1)
-CP_DECLARE_VARIANT(3, 2, 2)
-CP_DECLARE_VARIANT(3, 2, 3)
-CP_DECLARE_VARIANT(1, 1, 0)
-CP_DECLARE_VARIANT(1, 2, 0)
-CP_DECLARE_VARIANT(4, 1, 0)
-CP_DECLARE_VARIANT(4, 2, 0)
+// Single-stack outlier kernels specialised at compile time (cp_kernels_variant.cu, one
+// translation unit each): (channels, distance kind k: 1 integer / 2 paired f32 / 3 scalar
+// f32, outlier group g: 0 any / 1 extreme, first, last / 2 average / 3 forward, backward,
+// background b: 0 any / 1 first). RGB has one kernel per (k, g, b) for k = 1, 2; the other
+// cases one per kind. build.py compiles the same list.
+#define CP_VARIANTS(X)                                                                       \
+  X(3, 1, 1, 1) X(3, 1, 2, 1) X(3, 1, 3, 1) X(3, 1, 1, 0) X(3, 1, 2, 0) X(3, 1, 3, 0)       \
+  X(3, 2, 1, 1) X(3, 2, 2, 1) X(3, 2, 3, 1) X(3, 2, 1, 0) X(3, 2, 2, 0) X(3, 2, 3, 0)       \
+  X(3, 3, 0, 0) X(1, 1, 0, 0) X(1, 2, 0, 0) X(1, 3, 0, 0) X(4, 1, 0, 0) X(4, 2, 0, 0)       \
+  X(4, 3, 0, 0)
+#define CP_DECLARE_VARIANT(CH, K, G, B)                                                      \
+  int launch_composite_c##CH##_k##K##_g##G##_b##B(const StackDev& s, int grid, int smem,    \
+                                                  void* stream, uint32_t* error);           \
+  int max_ctas_c##CH##_k##K##_g##G##_b##B(int threads, int smem);
+CP_VARIANTS(CP_DECLARE_VARIANT)
 #undef CP_DECLARE_VARIANT
 // Outlier group of a stack's outlier mode.
 inline int outlier_group(int outlier) {
   return outlier == CP_OUTLIER_AVERAGE ? 2
          : (outlier == CP_OUTLIER_FORWARD || outlier == CP_OUTLIER_BACKWARD) ? 3 : 1;
 }
+// The specialised kernel (k, g, b) an outlier stack launches with.
+inline void outlier_variant(const StackDev& s, int* k, int* g, int* b) {
+  *k = s.fast_int ? 1 : (s.pair_f32 ? 2 : 3);
+  const bool split = s.channels == 3 && *k != 3;
+  *g = split ? outlier_group(s.outlier) : 0;
+  *b = split && s.background == CP_BG_FIRST ? 1 : 0;
+}
 // Which single-stack kernel a stack launches with (an occupancy cache key).
-inline int single_variant(int mode, uint32_t fast_int, int outlier) {
-  return mode != CP_MODE_OUTLIER ? 0 : (fast_int ? 1 : 2) * 4 + outlier_group(outlier);
+inline int single_variant(const StackDev& s) {
+  if (s.mode != CP_MODE_OUTLIER) return 0;
+  int k, g, b;
+  outlier_variant(s, &k, &g, &b);
+  return 1 + k * 8 + g * 2 + b;
 }
 
 // Shake search (cp_shake.cu): diffs[(f-1) * S^2 + oy*S + ox] for frames 1..n-1.

@@ -4,7 +4,7 @@
 namespace cp {
 
 int composite_max_ctas_c3(int threads, int smem) {
-  const void* fn = reinterpret_cast<const void*>(&k_composite<3, kAnyKind, kOgAny>);
+  const void* fn = reinterpret_cast<const void*>(&k_composite<3, kAnyKind, kOgAny, kBgAny>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess)
@@ -12,32 +12,10 @@ int composite_max_ctas_c3(int threads, int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
-int single_max_ctas_c3(const StackDev& s, int smem) {
-  if (s.mode == CP_MODE_OUTLIER) {
-    const int g = outlier_group(s.outlier);
-    if (s.fast_int)
-      return g == 1 ? max_ctas_c3_k1_g1(s.threads, smem)
-             : g == 2 ? max_ctas_c3_k1_g2(s.threads, smem) : max_ctas_c3_k1_g3(s.threads, smem);
-    return g == 1 ? max_ctas_c3_k2_g1(s.threads, smem)
-           : g == 2 ? max_ctas_c3_k2_g2(s.threads, smem) : max_ctas_c3_k2_g3(s.threads, smem);
-  }
-  return max_ctas_kind<3, kAnyKind, kOgAny>(s.threads, smem);
-}
-
-// Outlier stacks go to the kernel of their distance arithmetic (and, for RGB, outlier group),
-// the rest to the general one.
+// The general kernel (single-stack launches of darker / lighter stacks the streaming kernel
+// does not take); outlier stacks launch a specialised kernel (cp_kernels_variant.cu).
 int launch_composite_c3(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
-  if (s.mode == CP_MODE_OUTLIER) {
-    const int g = outlier_group(s.outlier);
-    if (s.fast_int)
-      return g == 1 ? launch_composite_c3_k1_g1(s, grid, smem, stream, error)
-             : g == 2 ? launch_composite_c3_k1_g2(s, grid, smem, stream, error)
-                      : launch_composite_c3_k1_g3(s, grid, smem, stream, error);
-    return g == 1 ? launch_composite_c3_k2_g1(s, grid, smem, stream, error)
-           : g == 2 ? launch_composite_c3_k2_g2(s, grid, smem, stream, error)
-                    : launch_composite_c3_k2_g3(s, grid, smem, stream, error);
-  }
-  return launch_composite_kind<3, kAnyKind, kOgAny>(s, grid, smem, stream, error);
+  return launch_composite_kind<3, kAnyKind, kOgAny, kBgAny>(s, grid, smem, stream, error);
 }
 
 int launch_batch_c3(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks,

@@ -574,13 +574,20 @@ DEVI void store_rows(uint8_t* out, const TileGeo& g, const uint32_t (&rows)[C][3
 // Kernel kinds: kAnyKind handles every stack (batches mix them); a single-stack launch takes
 // the kind of its distance arithmetic, so each kernel holds only the code it runs (smaller
 // instruction footprint, register allocation of its own).
-// Likewise the outlier group (OG) fixes the epilogue: kOgSingle (extreme / first / last: one
-// sample), kOgAverage, kOgBlend (forward / backward), or kOgAny.
-enum : int { kAnyKind = 0, kIntKind = 1, kF32Kind = 2 };
+// Kinds: kIntKind (abs, 0/1 weights: integer distances), kF32Kind (paired f32 distances),
+// kF32GenKind (scalar f32 distances). Likewise the outlier group (OG) fixes the epilogue:
+// kOgSingle (extreme / first / last: one sample), kOgAverage, kOgBlend (forward / backward),
+// or kOgAny; and BG the background: kBgFirst or kBgAny.
+enum : int { kAnyKind = 0, kIntKind = 1, kF32Kind = 2, kF32GenKind = 3 };
 enum : int { kOgAny = 0, kOgSingle = 1, kOgAverage = 2, kOgBlend = 3 };
+enum : int { kBgAny = 0, kBgFirst = 1 };
 template <int KIND>
 DEVI bool fast_path(const StackDev& S) {
-  return KIND == kIntKind ? true : (KIND == kF32Kind ? false : S.fast_int != 0);
+  return KIND == kIntKind ? true : (KIND == kAnyKind ? S.fast_int != 0 : false);
+}
+template <int KIND>
+DEVI bool pair_path(const StackDev& S) {
+  return KIND == kF32Kind ? true : (KIND == kAnyKind ? S.pair_f32 != 0 : false);
 }
 template <int OG>
 DEVI bool og_is(const StackDev& S, int og) {
@@ -591,7 +598,7 @@ DEVI bool og_is(const StackDev& S, int og) {
   return m == CP_OUTLIER_EXTREME || m == CP_OUTLIER_FIRST || m == CP_OUTLIER_LAST;
 }
 
-template <int C, int NW, bool SH, int KIND, int OG>
+template <int C, int NW, bool SH, int KIND, int OG, int BG>
 DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
                        Aux<C, NW>& A, uint32_t& warn_count) {
   constexpr int BP = NW <= 2 ? 4 : 2;  // byte positions per plane build (register budget)
@@ -739,7 +746,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
             kmax[p] = max(kmax[p], (d << 8) + fk);
           }
         }
-      } else if (S.pair_f32) {
+      } else if (pair_path<KIND>(S)) {
         // pixels (0, 1) and (2, 3) in float2 lanes, every term on (median - p) / 2: the
         // sample -(2^14 + p/2) is one byte permute of the pixel byte into -2^14's mantissa,
         // the median 2^14 + median/2 is exact, and their sum is exactly (median - p) / 2.
@@ -827,7 +834,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
       // the paired pass kept distances / 4: scale back exactly
       A.best[wp][p][t] =
           fast ? kmax[p]
-               : __float_as_int(S.pair_f32 ? __fmul_rn(dmax_f[p], 4.0f) : dmax_f[p]);
+               : __float_as_int(pair_path<KIND>(S) ? __fmul_rn(dmax_f[p], 4.0f) : dmax_f[p]);
       A.imf[wp][p][t] = imax[p];
     }
   }
@@ -877,12 +884,13 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     int nout = 0;
 #pragma unroll
     for (int w = 0; w < NW; ++w) nout += __popc(pb[w]);
+    const int bgm = BG == kBgFirst ? CP_BG_FIRST : S.background;
     bool warning = false;
     int bg_idx = -1;
     uint32_t pix = 0;
     // background, src/chrono.rs:293-375
-    if (S.background == CP_BG_FIRST || S.background == CP_BG_RANDOM) {
-      if (S.background == CP_BG_FIRST) {
+    if (bgm == CP_BG_FIRST || bgm == CP_BG_RANDOM) {
+      if (bgm == CP_BG_FIRST) {
         if (nout == 0) {
           bg_idx = 0;
         } else if (nout == n) {
@@ -922,7 +930,7 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
         }
       }
       pix = load_pixel<C, SH>(rd, bg_idx, p);
-    } else if (S.background == CP_BG_AVERAGE) {
+    } else if (bgm == CP_BG_AVERAGE) {
       uint32_t sum[C];
 #pragma unroll
       for (int ch = 0; ch < C; ++ch) sum[ch] = 0u;
@@ -1149,21 +1157,21 @@ DEVI void simple_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd
 }
 
 // Kinds other than kAnyKind only run outlier stacks.
-template <int C, bool SH, int KIND, int OG>
+template <int C, bool SH, int KIND, int OG, int BG>
 DEVI void process_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
                        uint8_t* aux, uint32_t& warn) {
   if (S.nw == 1) {
     Aux<C, 1>& A = *reinterpret_cast<Aux<C, 1>*>(aux);
     if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 1, SH>(S, g, rd, A);
-    else outlier_tile<C, 1, SH, KIND, OG>(S, g, rd, A, warn);
+    else outlier_tile<C, 1, SH, KIND, OG, BG>(S, g, rd, A, warn);
   } else if (S.nw == 2) {
     Aux<C, 2>& A = *reinterpret_cast<Aux<C, 2>*>(aux);
     if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 2, SH>(S, g, rd, A);
-    else outlier_tile<C, 2, SH, KIND, OG>(S, g, rd, A, warn);
+    else outlier_tile<C, 2, SH, KIND, OG, BG>(S, g, rd, A, warn);
   } else {
     Aux<C, 4>& A = *reinterpret_cast<Aux<C, 4>*>(aux);
     if (KIND == kAnyKind && S.mode != CP_MODE_OUTLIER) simple_tile<C, 4, SH>(S, g, rd, A);
-    else outlier_tile<C, 4, SH, KIND, OG>(S, g, rd, A, warn);
+    else outlier_tile<C, 4, SH, KIND, OG, BG>(S, g, rd, A, warn);
   }
 }
 
@@ -1196,7 +1204,7 @@ DEVI void load_fbase(const StackDev& S, const SmemLayout& L) {
 
 // Stage a tile, wait for it (bounded) and process it. Returns false after a timed-out wait.
 // The exchange area sits behind the n staged rows.
-template <int C, int KIND, int OG>
+template <int C, int KIND, int OG, int BG>
 DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uint32_t& phase,
                    uint32_t* error, uint32_t& warn) {
   if (threadIdx.x < 32) {
@@ -1213,17 +1221,17 @@ DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uin
   uint8_t* aux = L.buf + static_cast<size_t>(S.n) * kPitch<C>;
   if (S.shifted) {
     const Rows<C, true> rd{col, L.shifts};
-    process_tile<C, true, KIND, OG>(S, g, rd, aux, warn);
+    process_tile<C, true, KIND, OG, BG>(S, g, rd, aux, warn);
   } else {
     const Rows<C, false> rd{col, L.shifts};
-    process_tile<C, false, KIND, OG>(S, g, rd, aux, warn);
+    process_tile<C, false, KIND, OG, BG>(S, g, rd, aux, warn);
   }
   __syncthreads();
   return true;
 }
 
 // One stack, persistent CTAs (C warps each) striding over its tiles.
-template <int C, int KIND, int OG>
+template <int C, int KIND, int OG, int BG>
 __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_constant__ StackDev S,
                                                       uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -1236,13 +1244,13 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite(const __grid_
   __syncthreads();
   uint32_t phase = 0, warn = 0;
   for (int t = blockIdx.x; t < S.tiles; t += gridDim.x)
-    if (!run_tile<C, KIND, OG>(S, tile_geo(S, t), L, phase, error, warn)) return;
+    if (!run_tile<C, KIND, OG, BG>(S, tile_geo(S, t), L, phase, error, warn)) return;
   flush_warnings(S.warnings, warn);
 }
 
-template <int C, int KIND, int OG>
+template <int C, int KIND, int OG, int BG>
 int max_ctas_kind(int threads, int smem) {
-  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND, OG>);
+  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND, OG, BG>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, threads, smem) != cudaSuccess)
@@ -1250,11 +1258,11 @@ int max_ctas_kind(int threads, int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
-template <int C, int KIND, int OG>
+template <int C, int KIND, int OG, int BG>
 int launch_composite_kind(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
-  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND, OG>);
+  const void* fn = reinterpret_cast<const void*>(&k_composite<C, KIND, OG, BG>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_composite<C, KIND, OG><<<grid, s.threads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
+  k_composite<C, KIND, OG, BG><<<grid, s.threads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -1304,7 +1312,7 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const S
       __syncthreads();
     }
     uint32_t warn = 0;
-    if (!run_tile<C, kAnyKind, kOgAny>(S, tile_geo(S, tile), L, phase, error, warn)) return;
+    if (!run_tile<C, kAnyKind, kOgAny, kBgAny>(S, tile_geo(S, tile), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
   }
 }
