@@ -29,6 +29,8 @@ CU_SOURCES = ["cp_kernels_c3.cu", "cp_kernels_c4.cu", "cp_kernels_c1.cu", "cp_sh
 KERNEL_VARIANTS = [(3, k, g, b) for k in (1, 2) for b in (1, 0) for g in (1, 2, 3)] + \
     [(3, 3, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0), (1, 3, 0, 0), (4, 1, 0, 0), (4, 2, 0, 0),
      (4, 3, 0, 0)]
+# cp_kernels_batch_variant.cu: the CP_BATCH_VARIANTS list of cp_internal.h
+BATCH_VARIANTS = [(3, k, g, 1) for k in (1, 2) for g in (1, 2, 3)]
 CPP_SOURCES = ["cp_host.cpp", "cp_stage.cpp", "cp_batch.cpp", "cp_shake_host.cpp",
                "cp_server.cpp"]
 HEADERS = ["cp_internal.h", "cp_host_internal.h", "cp_tile.cuh"]
@@ -79,6 +81,14 @@ def build(verbose=False, jobs=None):
             steps.append([nvcc] + ARCH + NVCC_FLAGS + [
                 "-DCP_CH=%d" % ch, "-DCP_KIND=%d" % kind, "-DCP_OG=%d" % og, "-DCP_BG=%d" % bg,
                 "-c", vsrc, "-o", o])
+    bsrc = os.path.join(CSRC, "cp_kernels_batch_variant.cu")
+    for ch, kind, og, bg in BATCH_VARIANTS:
+        o = os.path.join(OBJ_DIR, "cp_kernels_batch_c%d_k%d_g%d_b%d.o" % (ch, kind, og, bg))
+        objs.append(o)
+        if _stale(o, [bsrc] + hdrs):
+            steps.append([nvcc] + ARCH + NVCC_FLAGS + [
+                "-DCP_CH=%d" % ch, "-DCP_KIND=%d" % kind, "-DCP_OG=%d" % og, "-DCP_BG=%d" % bg,
+                "-c", bsrc, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ_DIR, src + ".o")

@@ -30,6 +30,28 @@ void release_plans(cp_ctx* ctx) {
   ctx->plans.clear();
 }
 
+// The specialised batched kernel every stack of the batch would take, if there is one.
+static bool uniform_variant(const std::vector<StackDev>& host, int* k, int* g, int* b) {
+  for (size_t i = 0; i < host.size(); ++i) {
+    const StackDev& d = host[i];
+    if (d.mode != CP_MODE_OUTLIER || d.channels != 3) return false;
+    int ki, gi, bi;
+    outlier_variant(d, &ki, &gi, &bi);
+    if (i == 0) {
+      *k = ki;
+      *g = gi;
+      *b = bi;
+    } else if (ki != *k || gi != *g || bi != *b) {
+      return false;
+    }
+  }
+  bool listed = false;
+#define CP_BATCH_LISTED(CH, K, G, B) listed = listed || (*k == K && *g == G && *b == B);
+  CP_BATCH_VARIANTS(CP_BATCH_LISTED)
+#undef CP_BATCH_LISTED
+  return listed;
+}
+
 static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_n,
                             cudaStream_t st) {
   const int n_stacks = static_cast<int>(plan.host.size());
@@ -37,16 +59,35 @@ static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_
   int32_t* d_prefix = reinterpret_cast<int32_t*>(d_stacks + n_stacks);
   uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + n_stacks + 1);
   const int smem = smem_bytes_for(max_n, channels);
+  int k = 0, g = 0, b = 0;
+  const bool uniform = uniform_variant(plan.host, &k, &g, &b);
   int per_sm = 1;
-  switch (channels) {
-    case 1: per_sm = composite_max_ctas_c1(cta_threads(1), smem); break;
-    case 3: per_sm = composite_max_ctas_c3(cta_threads(3), smem); break;
-    default: per_sm = composite_max_ctas_c4(cta_threads(4), smem); break;
+  if (uniform) {
+#define CP_BATCH_OCC(CH, K, G, B) \
+  if (k == K && g == G && b == B) per_sm = batch_max_ctas_c##CH##_k##K##_g##G##_b##B(smem);
+    CP_BATCH_VARIANTS(CP_BATCH_OCC)
+#undef CP_BATCH_OCC
+  } else {
+    switch (channels) {
+      case 1: per_sm = composite_max_ctas_c1(cta_threads(1), smem); break;
+      case 3: per_sm = composite_max_ctas_c3(cta_threads(3), smem); break;
+      default: per_sm = composite_max_ctas_c4(cta_threads(4), smem); break;
+    }
   }
   const int grid = std::max(1, std::min(plan.total, per_sm * ctx->sm_count));
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_status(ctx, e, "memset");
   int rc = 0;
+  if (uniform) {
+#define CP_BATCH_LAUNCH(CH, K, G, B)                                                        \
+  if (k == K && g == G && b == B)                                                           \
+    rc = launch_batch_c##CH##_k##K##_g##G##_b##B(d_stacks, d_prefix, n_stacks, plan.total,  \
+                                                 plan.interleave, d_counter, ctx->d_error, \
+                                                 grid, smem, st);
+    CP_BATCH_VARIANTS(CP_BATCH_LAUNCH)
+#undef CP_BATCH_LAUNCH
+    return cuda_status(ctx, static_cast<cudaError_t>(rc), "batch launch");
+  }
   switch (channels) {
     case 1: rc = launch_batch_c1(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;
     case 3: rc = launch_batch_c3(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;

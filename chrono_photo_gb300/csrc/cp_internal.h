@@ -135,6 +135,18 @@ CP_DECLARE_CH(4)
   int max_ctas_c##CH##_k##K##_g##G##_b##B(int threads, int smem);
 CP_VARIANTS(CP_DECLARE_VARIANT)
 #undef CP_DECLARE_VARIANT
+// Batched kernels for uniform RGB batches with background first (cp_kernels_batch_variant.cu).
+#define CP_BATCH_VARIANTS(X)                                                                 \
+  X(3, 1, 1, 1) X(3, 1, 2, 1) X(3, 1, 3, 1) X(3, 2, 1, 1) X(3, 2, 2, 1) X(3, 2, 3, 1)
+#define CP_DECLARE_BATCH_VARIANT(CH, K, G, B)                                                \
+  int launch_batch_c##CH##_k##K##_g##G##_b##B(const StackDev* stacks, const int32_t* prefix,\
+                                              int32_t n_stacks, int32_t total,              \
+                                              int32_t interleave, uint32_t* counter,        \
+                                              uint32_t* error, int grid, int smem,          \
+                                              void* stream);                                \
+  int batch_max_ctas_c##CH##_k##K##_g##G##_b##B(int smem);
+CP_BATCH_VARIANTS(CP_DECLARE_BATCH_VARIANT)
+#undef CP_DECLARE_BATCH_VARIANT
 // Outlier group of a stack's outlier mode.
 inline int outlier_group(int outlier) {
   return outlier == CP_OUTLIER_AVERAGE ? 2

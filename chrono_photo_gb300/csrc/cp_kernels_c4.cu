@@ -21,11 +21,9 @@ int launch_composite_c4(const StackDev& s, int grid, int smem, void* stream, uin
 int launch_batch_c4(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks,
                      int32_t total, int32_t interleave, uint32_t* counter, uint32_t* error,
                      int grid, int smem, void* stream) {
-  cudaFuncSetAttribute(reinterpret_cast<const void*>(&k_composite_batch<4>),
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_composite_batch<4><<<grid, 32 * 4, smem, static_cast<cudaStream_t>(stream)>>>(
-      stacks, prefix, n_stacks, total, interleave, counter, error);
-  return static_cast<int>(cudaGetLastError());
+  return launch_batch_kind<4, kAnyKind, kOgAny, kBgAny>(stacks, prefix, n_stacks, total,
+                                                         interleave, counter, error, grid, smem,
+                                                         stream);
 }
 
 int simple_stream_max_ctas_c4(bool fast) {

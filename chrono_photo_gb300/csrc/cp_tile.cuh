@@ -1266,8 +1266,10 @@ int launch_composite_kind(const StackDev& s, int grid, int smem, void* stream, u
   return static_cast<int>(cudaGetLastError());
 }
 
-// Many stacks: persistent CTAs pull (stack, tile) items from a device counter.
-template <int C>
+// Many stacks: persistent CTAs pull (stack, tile) items from a device counter. A batch whose
+// stacks all take one specialised variant (chrono-video windows share their settings) runs
+// that variant; mixed batches the general kernel.
+template <int C, int KIND, int OG, int BG>
 __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const StackDev* __restrict__ stacks,
                                                             const int32_t* __restrict__ prefix,
                                                             int32_t n_stacks, int32_t total,
@@ -1312,9 +1314,30 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const S
       __syncthreads();
     }
     uint32_t warn = 0;
-    if (!run_tile<C, kAnyKind, kOgAny, kBgAny>(S, tile_geo(S, tile), L, phase, error, warn)) return;
+    if (!run_tile<C, KIND, OG, BG>(S, tile_geo(S, tile), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
   }
+}
+
+template <int C, int KIND, int OG, int BG>
+int batch_max_ctas_kind(int smem) {
+  const void* fn = reinterpret_cast<const void*>(&k_composite_batch<C, KIND, OG, BG>);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, 32 * C, smem) != cudaSuccess)
+    return 1;
+  return blocks < 1 ? 1 : blocks;
+}
+
+template <int C, int KIND, int OG, int BG>
+int launch_batch_kind(const StackDev* stacks, const int32_t* prefix, int32_t n_stacks,
+                      int32_t total, int32_t interleave, uint32_t* counter, uint32_t* error,
+                      int grid, int smem, void* stream) {
+  const void* fn = reinterpret_cast<const void*>(&k_composite_batch<C, KIND, OG, BG>);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  k_composite_batch<C, KIND, OG, BG><<<grid, 32 * C, smem, static_cast<cudaStream_t>(stream)>>>(
+      stacks, prefix, n_stacks, total, interleave, counter, error);
+  return static_cast<int>(cudaGetLastError());
 }
 
 // darker/lighter streaming over an aligned, uncropped stack: a CTA of 128 threads owns chunks
