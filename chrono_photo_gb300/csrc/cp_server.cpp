@@ -5,7 +5,10 @@
 // jobs and one worker thread that, on every turn:
 //   1. admits queued jobs while launch slots and HBM budget allow: reserves device memory,
 //      reuses frames already resident under the same caller key (shared windows), and
-//      issues the host->device copies of the rest on a copy stream;
+//      issues the host->device copies of the rest on two copy streams (frames alternate:
+//      one stream of back-to-back copies leaves the host link idle between copies). Device
+//      memory comes from a stream-ordered pool (cudaMallocFromPoolAsync / cudaFreeAsync), so
+//      admitting and retiring jobs never synchronises the device;
 //   2. gathers every admitted job whose frames have landed and runs all their tiles in one
 //      persistent batched launch (per channel count) on the next of several compute streams,
 //      so launches of newer jobs overlap older ones still on the device;
@@ -47,6 +50,26 @@ double now_s() {
 
 uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
 
+// Stream-ordered device memory from the server's pool, counted against the context budget.
+int pool_alloc(cp_ctx* ctx, cudaMemPool_t pool, uint64_t bytes, cudaStream_t st, void** p) {
+  *p = nullptr;
+  int rc = budget_reserve(ctx, bytes);
+  if (rc) return rc;
+  const cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, st);
+  if (e != cudaSuccess) {
+    budget_release(ctx, bytes);
+    *p = nullptr;
+    return cuda_status(ctx, e, "cudaMallocFromPoolAsync");
+  }
+  return CP_OK;
+}
+// The memory's last users have completed (the worker saw their events).
+void pool_free(cp_ctx* ctx, void* p, uint64_t bytes, cudaStream_t st) {
+  if (!p) return;
+  cudaFreeAsync(p, st);
+  budget_release(ctx, bytes);
+}
+
 struct Frame {  // a device frame, shared by key
   void* dev = nullptr;
   uint64_t bytes = 0;
@@ -74,6 +97,7 @@ struct Job {
   uint64_t stage_bytes = 0;
   uint64_t reserved = 0;
   int state = 0;  // 0 queued, 1 admitted (uploading), 2 launched, 3 done
+  cudaEvent_t staged = nullptr;   // own uploads and the warning-counter reset finished
   cudaEvent_t done_ev = nullptr;
   cp_job_result res{};
 };
@@ -101,7 +125,8 @@ struct cp_server {
   std::unordered_map<uint64_t, std::unique_ptr<Job>> jobs;  // by id
   std::unordered_map<uint64_t, std::unique_ptr<Frame>> cache;  // keyed frames
   cudaStream_t compute[kStreams] = {};
-  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaStream_t h2d = nullptr, h2d2 = nullptr, d2h = nullptr;
+  cudaMemPool_t pool = nullptr;  // frames and outputs
   int next_stream = 0;
   std::vector<LaunchSlot> slots;
   std::thread worker;
@@ -149,7 +174,7 @@ void evict_for(cp_server* srv, uint64_t need) {
     if (!bf) return;
     cudaEventSynchronize(bf->ready);
     cudaEventDestroy(bf->ready);
-    dev_free(srv->ctx, bf->dev);
+    pool_free(srv->ctx, bf->dev, bf->bytes, srv->h2d);
     srv->reserved -= bf->bytes;
     srv->cache.erase(best);
   }
@@ -160,6 +185,7 @@ int admit(cp_server* srv, Job* j) {
   const uint64_t pitch = frame_pitch_of(*j), fbytes = frame_bytes_of(*j);
   const int n = j->spec.stack.n;
   j->frames.assign(static_cast<size_t>(n), nullptr);
+  int uploads = 0;
   for (int i = 0; i < n; ++i) {
     const uint64_t k = j->keys.empty() ? 0 : j->keys[static_cast<size_t>(i)];
     Frame* f = nullptr;
@@ -169,14 +195,15 @@ int admit(cp_server* srv, Job* j) {
     }
     if (!f) {
       std::unique_ptr<Frame> nf(new Frame());
-      int rc = dev_alloc(ctx, pitch, &nf->dev);
+      cudaStream_t cs = (uploads++ & 1) ? srv->h2d2 : srv->h2d;
+      int rc = pool_alloc(ctx, srv->pool, pitch, cs, &nf->dev);
       if (rc) return rc;
       nf->bytes = pitch;
       srv->reserved += pitch;
       cudaEventCreateWithFlags(&nf->ready, cudaEventDisableTiming);
       cudaMemcpyAsync(nf->dev, j->host_frames[static_cast<size_t>(i)], fbytes,
-                      cudaMemcpyHostToDevice, srv->h2d);
-      cudaEventRecord(nf->ready, srv->h2d);
+                      cudaMemcpyHostToDevice, cs);
+      cudaEventRecord(nf->ready, cs);
       f = nf.get();
       if (k) {
         srv->cache[k] = std::move(nf);
@@ -191,7 +218,7 @@ int admit(cp_server* srv, Job* j) {
   }
   const uint64_t ob = out_bytes_of(*j);
   void* p = nullptr;
-  int rc = dev_alloc(ctx, 2 * ob + 256, &p);
+  int rc = pool_alloc(ctx, srv->pool, 2 * ob + 256, srv->h2d, &p);
   if (rc) return rc;
   srv->reserved += 2 * ob + 256;
   j->reserved = 2 * ob + 256;
@@ -199,6 +226,14 @@ int admit(cp_server* srv, Job* j) {
   j->blend_dev = static_cast<uint8_t*>(p) + ob;
   j->warn_dev = reinterpret_cast<unsigned long long*>(static_cast<uint8_t*>(p) + 2 * ob);
   cudaMemsetAsync(j->warn_dev, 0, 8, srv->h2d);
+  // staged: the reset above and this job's uploads on both copy streams
+  cudaEvent_t join = nullptr;
+  cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+  cudaEventRecord(join, srv->h2d2);
+  cudaStreamWaitEvent(srv->h2d, join, 0);
+  cudaEventDestroy(join);  // released once the recorded work completes
+  cudaEventCreateWithFlags(&j->staged, cudaEventDisableTiming);
+  cudaEventRecord(j->staged, srv->h2d);
   // device->host copies go to pinned staging (a copy into pageable memory would block the
   // worker until the launch finishes); the worker copies to the caller's buffers at the end
   j->stage_bytes = 2 * ob + 64;
@@ -222,16 +257,20 @@ void release(cp_server* srv, Job* j) {
     if (f) f->refs -= 1;
   for (Frame* f : j->private_frames) {
     cudaEventDestroy(f->ready);
-    dev_free(srv->ctx, f->dev);
+    pool_free(srv->ctx, f->dev, f->bytes, srv->h2d);
     srv->reserved -= f->bytes;
     delete f;
   }
   j->private_frames.clear();
   j->frames.clear();
   if (j->out_dev) {
-    dev_free(srv->ctx, j->out_dev);
+    pool_free(srv->ctx, j->out_dev, j->reserved, srv->h2d);
     srv->reserved -= j->reserved;
     j->out_dev = nullptr;
+  }
+  if (j->staged) {
+    cudaEventDestroy(j->staged);
+    j->staged = nullptr;
   }
   if (j->stage) {
     srv->pinned_free.emplace(j->stage_bytes, j->stage);
@@ -241,6 +280,11 @@ void release(cp_server* srv, Job* j) {
 
 // 1: every frame of the job is on the device; 0: copies still in flight; -1: a copy failed.
 int frames_ready(const Job* j) {
+  if (j->staged) {
+    const cudaError_t q = cudaEventQuery(j->staged);
+    if (q == cudaErrorNotReady) return 0;
+    if (q != cudaSuccess) return -1;
+  }
   for (const Frame* f : j->frames) {
     const cudaError_t q = cudaEventQuery(f->ready);
     if (q == cudaErrorNotReady) return 0;
@@ -468,8 +512,17 @@ int cp_server_create(cp_ctx* ctx, uint64_t hbm_budget, int32_t max_inflight, cp_
   for (auto& s : srv->compute)
     if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return CP_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&srv->h2d, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&srv->h2d2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&srv->d2h, cudaStreamNonBlocking) != cudaSuccess)
     return CP_ERR_CUDA;
+  cudaMemPoolProps props;
+  std::memset(&props, 0, sizeof props);
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = ctx->device;
+  if (cudaMemPoolCreate(&srv->pool, &props) != cudaSuccess) return CP_ERR_CUDA;
+  uint64_t keep = ~0ull;  // keep freed memory in the pool for later jobs (the budget bounds it)
+  cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   srv->slots.resize(static_cast<size_t>(kStreams) * 2);
   for (auto& s : srv->slots) cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming);
   srv->worker = std::thread(worker_loop, srv.get());
@@ -551,11 +604,13 @@ int cp_server_destroy(cp_server* srv) {
   cudaSetDevice(srv->ctx->device);
   for (auto& s : srv->compute) cudaStreamSynchronize(s);
   cudaStreamSynchronize(srv->h2d);
+  cudaStreamSynchronize(srv->h2d2);
   cudaStreamSynchronize(srv->d2h);
   for (auto& kv : srv->cache) {
     cudaEventDestroy(kv.second->ready);
-    dev_free(srv->ctx, kv.second->dev);
+    pool_free(srv->ctx, kv.second->dev, kv.second->bytes, srv->h2d);
   }
+  cudaStreamSynchronize(srv->h2d);
   for (auto& s : srv->slots) {
     if (s.dev) dev_free(srv->ctx, s.dev);
     if (s.pinned) cudaFreeHost(s.pinned);
@@ -564,7 +619,9 @@ int cp_server_destroy(cp_server* srv) {
   for (auto& kv : srv->pinned_free) cudaFreeHost(kv.second);
   for (auto& s : srv->compute) cudaStreamDestroy(s);
   cudaStreamDestroy(srv->h2d);
+  cudaStreamDestroy(srv->h2d2);
   cudaStreamDestroy(srv->d2h);
+  if (srv->pool) cudaMemPoolDestroy(srv->pool);
   const int err = srv->error;
   delete srv;
   return err;
