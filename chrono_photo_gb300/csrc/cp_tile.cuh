@@ -831,11 +831,15 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     for (int p = 0; p < 4; ++p) {
 #pragma unroll
       for (int w = 0; w < NW; ++w) A.bits[wp][p][w][t] = bits[p][w];
-      // the paired pass kept distances / 4: scale back exactly
-      A.best[wp][p][t] =
-          fast ? kmax[p]
-               : __float_as_int(pair_path<KIND>(S) ? __fmul_rn(dmax_f[p], 4.0f) : dmax_f[p]);
-      A.imf[wp][p][t] = imax[p];
+      // only `extreme` reads the largest distance: other outlier groups leave it (and, the
+      // compiler seeing it dead, its computation in the distance pass) out
+      if (OG == kOgAny || OG == kOgSingle) {
+        // the paired pass kept distances / 4: scale back exactly
+        A.best[wp][p][t] =
+            fast ? kmax[p]
+                 : __float_as_int(pair_path<KIND>(S) ? __fmul_rn(dmax_f[p], 4.0f) : dmax_f[p]);
+        A.imf[wp][p][t] = imax[p];
+      }
     }
   }
   __syncthreads();
@@ -847,21 +851,24 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     const bool valid = 4 * t + p < g.npx;
     // combine the frame classes: flags OR, integer key max, f32 (distance, earliest frame)
     uint32_t pb[NW];
-    int32_t key = A.best[0][p][t];
-    float pdmax_f = __int_as_float(A.best[0][p][t]);
-    int pimf = A.imf[0][p][t];
+    constexpr bool kMaxKept = OG == kOgAny || OG == kOgSingle;  // see the distance pass
+    int32_t key = kMaxKept ? A.best[0][p][t] : -1;
+    float pdmax_f = kMaxKept ? __int_as_float(A.best[0][p][t]) : 0.0f;
+    int pimf = kMaxKept ? A.imf[0][p][t] : 0;
 #pragma unroll
     for (int w = 0; w < NW; ++w) pb[w] = A.bits[0][p][w][t];
 #pragma unroll
     for (int c = 1; c < C; ++c) {
 #pragma unroll
       for (int w = 0; w < NW; ++w) pb[w] |= A.bits[c][p][w][t];
-      key = max(key, A.best[c][p][t]);
-      const float d = __int_as_float(A.best[c][p][t]);
-      const int fi = A.imf[c][p][t];
-      const bool better = d > pdmax_f || (d == pdmax_f && fi < pimf);
-      pdmax_f = better ? d : pdmax_f;
-      pimf = better ? fi : pimf;
+      if (kMaxKept) {
+        key = max(key, A.best[c][p][t]);
+        const float d = __int_as_float(A.best[c][p][t]);
+        const int fi = A.imf[c][p][t];
+        const bool better = d > pdmax_f || (d == pdmax_f && fi < pimf);
+        pdmax_f = better ? d : pdmax_f;
+        pimf = better ? fi : pimf;
+      }
     }
     const PixStats<C> ps = pixel_stats<C, NW>(S, A, t, p);
     const uint32_t pklo = ps.klo, pkhi = ps.khi;
