@@ -10,7 +10,7 @@
 //      and a 4x4 byte transpose, giving 8 bit planes of up to 32*NW frames per channel
 //      byte (frame i = bit i).
 //   3. Order statistics (median, quartiles) come from a radix select on the planes: 8 steps
-//      of popcounts on candidate masks; the next order statistic is the minimum above.
+//      of popcounts on candidate masks; a pair d[k], d[k+1] takes two passes.
 //   4. Distance pass over all frames: with an abs threshold and 0/1 weights the doubled
 //      distance is exact integer arithmetic, 4*(p-m)^2 = 4*|p-floor m|*|p-ceil m| + [m
 //      half-integer], one dp4a of two vabsdiff4 per pixel and frame; otherwise the f32
@@ -359,27 +359,21 @@ DEVI void build_planes(uint32_t (&P)[BP][8][NW], const Rows<C, SH>& rd, int w, i
   }
 }
 
-// Order statistics d[k] (lo) and, when `pair`, d[k+1] (hi), for BP positions at once
-// (independent chains the scheduler interleaves). One radix pass over the 8 bit planes finds
-// d[k]. Rank k+1 follows the same branches until the one step where the zero-count equals
-// rank k's remaining rank + 1: there k goes to the zero branch and k+1 to the one branch,
-// whose minimum is d[k+1]. Without such a step both end in the same run: d[k+1] = d[k].
+// Order statistic d[k] for BP byte positions at once (independent chains the scheduler
+// interleaves): one radix pass over the 8 bit planes, each step counting the candidates with
+// a 0 bit (POPC) and keeping the half that holds rank k. A pair d[k], d[k+1] is two passes:
+// measured cheaper than tracking the sibling branch of rank k+1 and walking it afterwards.
 template <int NW, int BP>
-DEVI void select_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], int k,
-                       bool pair, uint32_t (&lo)[BP], uint32_t (&hi)[BP]) {
-  uint32_t c[BP][NW], sib[BP][NW];
+DEVI void select_rank(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], int k,
+                      uint32_t (&v)[BP]) {
+  uint32_t c[BP][NW];
   int kk[BP];
-  bool split[BP];
 #pragma unroll
   for (int j = 0; j < BP; ++j) {
 #pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      c[j][w] = S[w];
-      sib[j][w] = 0u;
-    }
+    for (int w = 0; w < NW; ++w) c[j][w] = S[w];
     kk[j] = k;
-    lo[j] = 0u;
-    split[j] = false;
+    v[j] = 0u;
   }
 #pragma unroll
   for (int b = 7; b >= 0; --b) {
@@ -393,46 +387,12 @@ DEVI void select_multi(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], 
         cz += __popc(z[w]);
       }
       const bool one = kk[j] >= cz;
-      const bool sp = !split[j] && cz == kk[j] + 1;  // k -> 0 branch, k+1 -> 1 branch
 #pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        const uint32_t o = c[j][w] ^ z[w];  // c & P
-        sib[j][w] = sp ? o : sib[j][w];
-        c[j][w] = one ? o : z[w];
-      }
-      split[j] = split[j] || sp;
+      for (int w = 0; w < NW; ++w) c[j][w] = one ? (c[j][w] ^ z[w]) : z[w];  // c & P or c & ~P
       kk[j] -= one ? cz : 0;
-      lo[j] = (lo[j] << 1) | static_cast<uint32_t>(one);
+      v[j] = (v[j] << 1) | static_cast<uint32_t>(one);
     }
   }
-  bool any = false;
-#pragma unroll
-  for (int j = 0; j < BP; ++j) {
-    hi[j] = lo[j];
-    split[j] = split[j] && pair;
-    any |= split[j];
-  }
-  if (!__any_sync(0xffffffffu, any)) return;
-  uint32_t m[BP];  // minimum of the sibling set: take the 0 branch whenever it is non-empty
-#pragma unroll
-  for (int j = 0; j < BP; ++j) m[j] = 0u;
-#pragma unroll
-  for (int b = 7; b >= 0; --b)
-#pragma unroll
-    for (int j = 0; j < BP; ++j) {
-      uint32_t z[NW];
-      uint32_t nz = 0;
-#pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        z[w] = sib[j][w] & ~P[j][b][w];
-        nz |= z[w];
-      }
-#pragma unroll
-      for (int w = 0; w < NW; ++w) sib[j][w] = nz ? z[w] : sib[j][w];
-      m[j] = (m[j] << 1) | (nz ? 0u : 1u);
-    }
-#pragma unroll
-  for (int j = 0; j < BP; ++j) hi[j] = split[j] ? m[j] : lo[j];
 }
 
 // quantile() of src/chrono.rs:567-579 from its order statistics: (1-frac)*d[p1] +
@@ -618,35 +578,76 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
     for (int kp0 = 0; kp0 < 4; kp0 += BP) {
       uint32_t P[BP][8][NW];
       build_planes<C, NW, BP, SH>(P, rd, wp, kp0, n);
+      // d[k] (and d[k+1] of a pair) of the median, and for rel thresholds of Q1 and Q3,
+      // through one copy of the selection code per path: loops rather than inlined
+      // selections (measured faster; the instruction cache is the tighter resource). The
+      // loop shapes differ per kernel kind because each measured best for its kind.
       uint32_t a1[BP], b1[BP], a3[BP], b3[BP];
-      if (!rel) {
-        uint32_t lo[BP], hi[BP];
-        select_multi<NW, BP>(P, smask, S.med_k, S.med_pair != 0, lo, hi);
-#pragma unroll
-        for (int k = 0; k < BP; ++k) {
-          plo |= lo[k] << (8 * (kp0 + k));
-          phi |= hi[k] << (8 * (kp0 + k));
-        }
-      }
-      // rel thresholds: the median, Q1 and Q3 through one copy of the selection code (a
-      // loop rather than three inlined selections: measured faster, the instruction cache
-      // being the tighter resource)
+      if constexpr (KIND == kIntKind) {  // abs thresholds only
+        uint32_t mlo[BP], mhi[BP];
 #pragma unroll 1
-      for (int r = 0; r < (rel ? 3 : 0); ++r) {
-        const int kr = r == 0 ? S.med_k : (r == 1 ? S.q1_k : S.q3_k);
-        const int pr = r == 0 ? S.med_pair : (r == 1 ? S.q1_pair : S.q3_pair);
-        uint32_t lo[BP], hi[BP];
-        select_multi<NW, BP>(P, smask, kr, pr != 0, lo, hi);
+        for (int r = 0; r < 2; ++r) {
+          if (r == 1 && !S.med_pair) continue;
+          uint32_t v[BP];
+          select_rank<NW, BP>(P, smask, S.med_k + r, v);
+#pragma unroll
+          for (int k = 0; k < BP; ++k) {
+            mlo[k] = r == 0 ? v[k] : mlo[k];
+            mhi[k] = v[k];  // the successor, or the value itself without a pair
+          }
+        }
 #pragma unroll
         for (int k = 0; k < BP; ++k) {
-          if (r == 0) {
+          plo |= mlo[k] << (8 * (kp0 + k));
+          phi |= mhi[k] << (8 * (kp0 + k));
+        }
+      } else {
+        if (!rel) {
+          uint32_t lo[BP], hi[BP];
+#pragma unroll 1
+          for (int r = 0; r < (S.med_pair ? 2 : 1); ++r) {
+            uint32_t v[BP];
+            select_rank<NW, BP>(P, smask, S.med_k + r, v);
+#pragma unroll
+            for (int k = 0; k < BP; ++k) {
+              lo[k] = r == 0 ? v[k] : lo[k];
+              hi[k] = v[k];
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < BP; ++k) {
             plo |= lo[k] << (8 * (kp0 + k));
             phi |= hi[k] << (8 * (kp0 + k));
           }
-          a1[k] = r == 1 ? lo[k] : a1[k];
-          b1[k] = r == 1 ? hi[k] : b1[k];
-          a3[k] = lo[k];
-          b3[k] = hi[k];
+        }
+        uint32_t mlo[BP], mhi[BP];
+#pragma unroll 1
+        for (int r = 0; r < (rel ? 6 : 0); ++r) {
+          const int rk = r >> 1;  // 0 median, 1 Q1, 2 Q3; odd r: the successor d[k+1]
+          const int kr = rk == 0 ? S.med_k : (rk == 1 ? S.q1_k : S.q3_k);
+          const int pr = rk == 0 ? S.med_pair : (rk == 1 ? S.q1_pair : S.q3_pair);
+          if ((r & 1) && !pr) continue;
+          uint32_t v[BP];
+          select_rank<NW, BP>(P, smask, kr + (r & 1), v);
+#pragma unroll
+          for (int k = 0; k < BP; ++k) {
+            if (!(r & 1)) {
+              mlo[k] = rk == 0 ? v[k] : mlo[k];
+              a1[k] = rk == 1 ? v[k] : a1[k];
+              a3[k] = rk == 2 ? v[k] : a3[k];
+            }
+            // the successor, or the value itself when the rank has no pair
+            mhi[k] = rk == 0 ? v[k] : mhi[k];
+            b1[k] = rk == 1 ? v[k] : b1[k];
+            b3[k] = rk == 2 ? v[k] : b3[k];
+          }
+        }
+        if (rel) {
+#pragma unroll
+          for (int k = 0; k < BP; ++k) {
+            plo |= mlo[k] << (8 * (kp0 + k));
+            phi |= mhi[k] << (8 * (kp0 + k));
+          }
         }
       }
       if (rel) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
