@@ -409,7 +409,8 @@ DEVI float quantile_value(uint32_t lo, uint32_t hi, bool pair, float frac) {
 // mantissa of 2^22 (ulp 0.5) both are exact and their difference is exactly median - p.
 // The `diff == 0 -> 0` case needs no select when every w * iqr_inv is finite (FINITE), since
 // then t = wi * 0 = 0 and t * t = 0.
-template <int C, bool FINITE>
+// NEGW: some weight may be negative (the paired kind excludes them).
+template <int C, bool FINITE, bool NEGW = true>
 DEVI float dist_f32(const StackDev& S, const float (&medo)[C], const float (&wi)[C], uint32_t px) {
   float d = 0.0f;
 #pragma unroll
@@ -419,7 +420,7 @@ DEVI float dist_f32(const StackDev& S, const float (&medo)[C], const float (&wi)
       const float diff = __fsub_rn(medo[ch], v);
       const float t = __fmul_rn(wi[ch], diff);
       float term = __fmul_rn(t, t);
-      if (S.neg_w) term = __fmul_rn(rsignum(S.w[ch]), term);
+      if (NEGW && S.neg_w) term = __fmul_rn(rsignum(S.w[ch]), term);
       if constexpr (!FINITE) term = diff == 0.0f ? 0.0f : term;
       d = __fadd_rn(d, term);
     }
@@ -887,6 +888,8 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
       if (fast)
         return static_cast<float>(dist_int(px, wbytes, pklo, pkhi)) +
                0.25f * static_cast<float>(pnh);
+      // the paired kind runs only for finite, non-negative weights
+      if constexpr (KIND == kF32Kind) return dist_f32<C, true, false>(S, pmedo, pwi, px);
       return dist_f32<C, false>(S, pmedo, pwi, px);
     };
     int nout = 0;
