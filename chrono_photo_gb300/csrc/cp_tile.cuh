@@ -269,10 +269,11 @@ DEVI uint32_t load_pixel(const Rows<C, SH>& rd, int f, int p) {
   if constexpr (C == 1) {
     return (rd.word(f, 0) >> (8 * p)) & 0xFFu;
   } else if constexpr (C == 3) {
-    if (p == 0) return rd.word(f, 0) & 0x00FFFFFFu;
-    if (p == 1) return __funnelshift_r(rd.word(f, 0), rd.word(f, 1), 24) & 0x00FFFFFFu;
-    if (p == 2) return __funnelshift_r(rd.word(f, 1), rd.word(f, 2), 16) & 0x00FFFFFFu;
-    return rd.word(f, 2) >> 8;
+    // bytes 3p .. 3p+2 of the column: word 3p/4 shifted right by (3p mod 4) bytes, topped up
+    // from the next word (no branch on p)
+    const int q = 3 * p, w0 = q >> 2;
+    return __funnelshift_r(rd.word(f, w0), rd.word(f, min(w0 + 1, 2)), 8 * (q & 3)) &
+           0x00FFFFFFu;
   } else {
     return rd.word(f, p);
   }
@@ -1073,9 +1074,8 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
         float dist;
         uint32_t sample;
         {
-          uint32_t osum[C];
-#pragma unroll
-          for (int ch = 0; ch < C; ++ch) osum[ch] = 0u;
+          // channel sums in 16-bit lanes (n * 255 < 2^16): even bytes, odd bytes
+          uint32_t se = 0u, so = 0u;
           float mdist = 0.0f;
 #pragma unroll
           for (int w = 0; w < NW; ++w) {
@@ -1084,16 +1084,18 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
               const int f = 32 * w + __ffs(m) - 1;
               m &= m - 1;
               const uint32_t px = load_pixel<C, SH>(rd, f, p);
-#pragma unroll
-              for (int ch = 0; ch < C; ++ch) osum[ch] += (px >> (8 * ch)) & 0xFFu;
+              se += px & 0x00FF00FFu;
+              so += (px >> 8) & 0x00FF00FFu;
               mdist = __fadd_rn(mdist, __fsqrt_rn(dsq_px(px)));
             }
           }
           const float kf = static_cast<float>(nout);
           sample = 0;
 #pragma unroll
-          for (int ch = 0; ch < C; ++ch)
-            sample |= sat_u8(rround(__fdiv_rn(static_cast<float>(osum[ch]), kf))) << (8 * ch);
+          for (int ch = 0; ch < C; ++ch) {
+            const uint32_t os = ((ch & 1) ? so : se) >> (16 * (ch >> 1)) & 0xFFFFu;
+            sample |= sat_u8(rround(__fdiv_rn(static_cast<float>(os), kf))) << (8 * ch);
+          }
           si = 0;  // src/chrono.rs:467: the fade of an averaged outlier is taken at frame 0
           dist = __fdiv_rn(mdist, kf);
         }
