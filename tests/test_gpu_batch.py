@@ -93,6 +93,30 @@ def test_batch_matches_oracle(ctx):
             assert warn == ref[2]
 
 
+@pytest.mark.parametrize("kw", [
+    dict(threshold="abs/0.05/0.2", outlier="extreme"),
+    dict(threshold="abs/0.04/0.3", outlier="average"),
+    dict(threshold="abs/0.04/0.3", outlier="backward"),
+    dict(threshold="rel/2/4", outlier="first"),
+    dict(threshold="rel/1.5/3", outlier="average"),
+    dict(threshold="rel/1.5/3", outlier="forward"),
+], ids=lambda kw: kw["threshold"] + "-" + kw["outlier"])
+def test_uniform_batch_variants(ctx, kw):
+    """Batches whose RGB stacks share one setting (background first) run the specialised
+    batched kernel of that setting; uneven frame counts and sizes still mix inside it."""
+    rng = np.random.default_rng(7)
+    items = []
+    for n, (h, w) in [(9, (13, 40)), (32, (24, 70)), (48, (17, 129)), (64, (33, 50)), (90, (8, 60))]:
+        frames = cases.random_stack(rng, n, h, w, 3, n_spots=5)
+        items.append((frames, dict(mode="outlier", background="first", **kw), 0))
+    got = run_batch(ctx, items)
+    for (frames, k, off), (out, blend, warn) in zip(items, got):
+        ref = oracle.composite(frames, cases.params(**k), frame_offset=off)
+        cases.assert_close_u8(out, ref[0], what="batch composite")
+        cases.assert_close_u8(blend, ref[1], what="batch blend")
+        assert warn == ref[2]
+
+
 def test_video_windows_match_oracle(ctx):
     """Overlapping windows over one resident pool (stride 1 and 2) with an absolute fade,
     evaluated at each window's first index."""
