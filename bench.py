@@ -441,6 +441,19 @@ def run_video(args):
 
     with ClockSampler(local) as clk:
         ms = _time_device(ctx, lib, call, args.steps, args.warmup)
+    # the plain kernel on the same windows: one cp_composite_device launch per window
+    wstacks = []
+    for k in range(nwin):
+        ptrs = (ct.c_void_p * win)(*[frame_ptrs[k + i] for i in range(win)])
+        keep.append(ptrs)
+        wstacks.append(_abi.Stack(n=win, width=W, height=H, channels=C,
+                                  frames=ct.cast(ptrs, ct.POINTER(ct.c_void_p)), frame_offset=k))
+
+    def plain():
+        for k in range(nwin):
+            ctx.check(lib.cp_composite_device(ctx.handle, ct.byref(wstacks[k]), ct.byref(p),
+                                              outs[k], blends[k], None, None, None), "plain")
+    plain_ms = _time_device(ctx, lib, plain, max(1, args.steps // 4), 2)
     # end to end: upload the pool from pinned memory, composite, read every window back
     optr, _ = _pinned(ctx, lib, 2 * nwin * fb)
     e2e_steps = max(1, min(args.steps, 10))
@@ -462,6 +475,9 @@ def run_video(args):
     print(json.dumps({
         "workload": "video", "metric": METRIC, "value": mpxf / (ms / 1e3), "unit": METRIC,
         "ms_per_call": ms, "steps": args.steps, "warmup": args.warmup, "dtype": "u8",
+        "plain_kernel": {"value": mpxf / (plain_ms / 1e3), "unit": METRIC, "ms": plain_ms,
+                         "note": "one single-stack launch per window"},
+        "batched_over_plain": plain_ms / ms,
         "data": "synthetic (seeded drift + sine-path disk)",
         "config": {"pool": n_pool, "windows": nwin, "window": win, "width": W, "height": H,
                    "settings": "abs/0.05/0.2 extreme, background first"},
@@ -532,6 +548,35 @@ def run_serve(args):
             ctx.check(lib.cp_composite_batch_device(ctx.handle, stacks, prm, nb, outs, None,
                                                     None, None), "batch")
     kernel_ms = _time_device(ctx, lib, kernel_all, max(1, args.steps // 50), 1)
+    # the plain kernel on the same jobs: one single-stack launch per job
+    flat = []
+    for stacks, prm, outs, nb in batches:
+        for k in range(nb):
+            flat.append((stacks[k], prm[k], outs[k]))
+
+    def plain_all():
+        for st, pr, o in flat:
+            ctx.check(lib.cp_composite_device(ctx.handle, ct.byref(st), ct.byref(pr), o, None,
+                                              None, None, None), "plain")
+    plain_ms = _time_device(ctx, lib, plain_all, max(1, args.steps // 50), 1)
+    # where batching pays: the small (320x240) jobs alone, batched in one launch vs one each
+    small = [i for i, j in enumerate(jobs) if j["w"] * j["h"] <= 320 * 240]
+    s_st = (_abi.Stack * len(small))(*[flat[i][0] for i in small])
+    s_pr = (_abi.Params * len(small))(*[flat[i][1] for i in small])
+    s_out = (ct.c_void_p * len(small))(*[flat[i][2] for i in small])
+    small_mpxf = sum(mpx_job[i] for i in small)
+
+    def small_batched():
+        ctx.check(lib.cp_composite_batch_device(ctx.handle, s_st, s_pr, len(small), s_out, None,
+                                                None, None), "small batch")
+
+    def small_plain():
+        for i in small:
+            st, pr, o = flat[i]
+            ctx.check(lib.cp_composite_device(ctx.handle, ct.byref(st), ct.byref(pr), o, None,
+                                              None, None, None), "small plain")
+    small_b_ms = _time_device(ctx, lib, small_batched, 20, 2) if small else 0.0
+    small_p_ms = _time_device(ctx, lib, small_plain, 20, 2) if small else 0.0
     total_mpxf = sum(mpx_job)
     kernel_rate = total_mpxf / (kernel_ms / 1e3)
     # served: Poisson arrivals, mean inter-arrival = 0.5 x the mean kernel-only job time
@@ -562,6 +607,14 @@ def run_serve(args):
                        "max": float(lat.max())},
         "arrival_mean_gap_ms": mean_gap * 1e3,
         "kernel_only": {"value": kernel_rate, "unit": METRIC, "ms_all_jobs": kernel_ms},
+        "plain_kernel": {"value": total_mpxf / (plain_ms / 1e3), "unit": METRIC,
+                         "ms_all_jobs": plain_ms, "note": "one single-stack launch per job"},
+        "batched_over_plain": plain_ms / kernel_ms,
+        "small_jobs": {"jobs": len(small), "batched_ms": small_b_ms, "plain_ms": small_p_ms,
+                       "batched": small_mpxf / (small_b_ms / 1e3) if small_b_ms else None,
+                       "plain": small_mpxf / (small_p_ms / 1e3) if small_p_ms else None,
+                       "batched_over_plain": small_p_ms / small_b_ms if small_b_ms else None,
+                       "note": "the 320x240 jobs: one batched launch vs one launch per job"},
         "e2e": {"value": total_mpxf / wall, "unit": METRIC, "h2d_bytes_total": h2d,
                 "d2h_bytes_total": 2 * sum(j["w"] * j["h"] * C for j in jobs)},
         "dtype": "u8", "data": "synthetic (seeded; frames drawn from 16 per resolution)",

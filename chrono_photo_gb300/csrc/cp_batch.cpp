@@ -30,41 +30,41 @@ void release_plans(cp_ctx* ctx) {
   ctx->plans.clear();
 }
 
-// The specialised batched kernel every stack of the batch would take, if there is one.
-static bool uniform_variant(const std::vector<StackDev>& host, int* k, int* g, int* b) {
-  for (size_t i = 0; i < host.size(); ++i) {
-    const StackDev& d = host[i];
-    if (d.mode != CP_MODE_OUTLIER || d.channels != 3) return false;
-    int ki, gi, bi;
-    outlier_variant(d, &ki, &gi, &bi);
-    if (i == 0) {
-      *k = ki;
-      *g = gi;
-      *b = bi;
-    } else if (ki != *k || gi != *g || bi != *b) {
-      return false;
-    }
-  }
-  bool listed = false;
-#define CP_BATCH_LISTED(CH, K, G, B) listed = listed || (*k == K && *g == G && *b == B);
-  CP_BATCH_VARIANTS(CP_BATCH_LISTED)
-#undef CP_BATCH_LISTED
-  return listed;
+// Index in CP_BATCH_VARIANTS of the specialised batched kernel a stack takes, or -1 (the
+// general batched kernel).
+int batch_variant_key(const StackDev& d) {
+  if (d.mode != CP_MODE_OUTLIER || d.channels != 3) return -1;
+  int k, g, b;
+  outlier_variant(d, &k, &g, &b);
+  int idx = 0, key = -1;
+#define CP_BATCH_KEY(CH, K, G, B) \
+  if (k == K && g == G && b == B) key = idx; \
+  ++idx;
+  CP_BATCH_VARIANTS(CP_BATCH_KEY)
+#undef CP_BATCH_KEY
+  return key;
 }
 
-static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_n,
-                            cudaStream_t st) {
-  const int n_stacks = static_cast<int>(plan.host.size());
-  StackDev* d_stacks = static_cast<StackDev*>(plan.dev);
-  int32_t* d_prefix = reinterpret_cast<int32_t*>(d_stacks + n_stacks);
-  uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + n_stacks + 1);
+// Stacks of one group share a launch: same batched kernel and plane-word count.
+int batch_group_key(const StackDev& d) { return (batch_variant_key(d) + 1) * 8 + d.nw; }
+
+// One persistent launch over `n` stacks (descriptors and prefix sums already on the device):
+// the specialised batched kernel when every stack takes the same one, else the general one.
+int launch_batch_dispatch(cp_ctx* ctx, const std::vector<StackDev>& host, const StackDev* d_stacks,
+                          const int32_t* d_prefix, int32_t total, int32_t interleave,
+                          uint32_t* d_counter, int max_n, cudaStream_t st) {
+  const int n = static_cast<int>(host.size());
+  const int channels = host[0].channels;
   const int smem = smem_bytes_for(max_n, channels);
-  int k = 0, g = 0, b = 0;
-  const bool uniform = uniform_variant(plan.host, &k, &g, &b);
+  int key = batch_variant_key(host[0]);
+  for (const StackDev& d : host)
+    if (batch_variant_key(d) != key) key = -1;
   int per_sm = 1;
-  if (uniform) {
+  if (key >= 0) {
+    int idx = 0;
 #define CP_BATCH_OCC(CH, K, G, B) \
-  if (k == K && g == G && b == B) per_sm = batch_max_ctas_c##CH##_k##K##_g##G##_b##B(smem);
+  if (key == idx) per_sm = batch_max_ctas_c##CH##_k##K##_g##G##_b##B(smem); \
+  ++idx;
     CP_BATCH_VARIANTS(CP_BATCH_OCC)
 #undef CP_BATCH_OCC
   } else {
@@ -74,26 +74,36 @@ static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int channels, int max_
       default: per_sm = composite_max_ctas_c4(cta_threads(4), smem); break;
     }
   }
-  const int grid = std::max(1, std::min(plan.total, per_sm * ctx->sm_count));
+  const int grid = std::max(1, std::min(total, per_sm * ctx->sm_count));
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_status(ctx, e, "memset");
   int rc = 0;
-  if (uniform) {
-#define CP_BATCH_LAUNCH(CH, K, G, B)                                                        \
-  if (k == K && g == G && b == B)                                                           \
-    rc = launch_batch_c##CH##_k##K##_g##G##_b##B(d_stacks, d_prefix, n_stacks, plan.total,  \
-                                                 plan.interleave, d_counter, ctx->d_error, \
-                                                 grid, smem, st);
+  if (key >= 0) {
+    int idx = 0;
+#define CP_BATCH_LAUNCH(CH, K, G, B)                                                          \
+  if (key == idx)                                                                             \
+    rc = launch_batch_c##CH##_k##K##_g##G##_b##B(d_stacks, d_prefix, n, total, interleave,   \
+                                                 d_counter, ctx->d_error, grid, smem, st);   \
+  ++idx;
     CP_BATCH_VARIANTS(CP_BATCH_LAUNCH)
 #undef CP_BATCH_LAUNCH
-    return cuda_status(ctx, static_cast<cudaError_t>(rc), "batch launch");
-  }
-  switch (channels) {
-    case 1: rc = launch_batch_c1(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;
-    case 3: rc = launch_batch_c3(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;
-    default: rc = launch_batch_c4(d_stacks, d_prefix, n_stacks, plan.total, plan.interleave, d_counter, ctx->d_error, grid, smem, st); break;
+  } else {
+    switch (channels) {
+      case 1: rc = launch_batch_c1(d_stacks, d_prefix, n, total, interleave, d_counter, ctx->d_error, grid, smem, st); break;
+      case 3: rc = launch_batch_c3(d_stacks, d_prefix, n, total, interleave, d_counter, ctx->d_error, grid, smem, st); break;
+      default: rc = launch_batch_c4(d_stacks, d_prefix, n, total, interleave, d_counter, ctx->d_error, grid, smem, st); break;
+    }
   }
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "batch launch");
+}
+
+static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int max_n, cudaStream_t st) {
+  const int n_stacks = static_cast<int>(plan.host.size());
+  StackDev* d_stacks = static_cast<StackDev*>(plan.dev);
+  int32_t* d_prefix = reinterpret_cast<int32_t*>(d_stacks + n_stacks);
+  uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + n_stacks + 1);
+  return launch_batch_dispatch(ctx, plan.host, d_stacks, d_prefix, plan.total, plan.interleave,
+                               d_counter, max_n, st);
 }
 
 }  // namespace cp
@@ -132,6 +142,42 @@ static int batch_run(cp_ctx* ctx, const cp_stack* stacks, const cp_params* param
   }
   if (smem_bytes_for(max_n, channels) > ctx->max_smem) return CP_ERR_ARG;
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+
+  // stacks that take different specialised batched kernels, or need shared memory for a
+  // different number of plane words (a launch sizes every CTA for its largest stack: one
+  // 128-frame stack among 16-frame ones would halve the residency of all), run as one launch
+  // per group, each group a plan of its own
+  std::vector<int> keys(static_cast<size_t>(n_stacks));
+  bool mixed = false;
+  for (int i = 0; i < n_stacks; ++i) {
+    const StackDev& d = host[static_cast<size_t>(i)];
+    keys[static_cast<size_t>(i)] = batch_group_key(d);
+    if (keys[static_cast<size_t>(i)] != keys[0]) mixed = true;
+  }
+  if (mixed) {
+    std::vector<int> distinct(keys);
+    std::sort(distinct.begin(), distinct.end());
+    distinct.erase(std::unique(distinct.begin(), distinct.end()), distinct.end());
+    for (int key : distinct) {
+      std::vector<cp_stack> gs;
+      std::vector<cp_params> gp;
+      std::vector<uint8_t*> go, gb;
+      std::vector<uint64_t*> gw;
+      for (int i = 0; i < n_stacks; ++i) {
+        if (keys[static_cast<size_t>(i)] != key) continue;
+        gs.push_back(stacks[i]);
+        gp.push_back(params[i]);
+        go.push_back(outs[i]);
+        gb.push_back(out_blends ? out_blends[i] : nullptr);
+        gw.push_back(warn_ptrs ? warn_ptrs[i] : nullptr);
+      }
+      const int rc = batch_run(ctx, gs.data(), gp.data(), static_cast<int32_t>(gs.size()),
+                               go.data(), out_blends ? gb.data() : nullptr,
+                               warn_ptrs ? gw.data() : nullptr, stream);
+      if (rc) return rc;
+    }
+    return CP_OK;
+  }
 
   // find a plan with the same descriptors
   BatchPlan* plan = nullptr;
@@ -178,7 +224,7 @@ static int batch_run(cp_ctx* ctx, const cp_stack* stacks, const cp_params* param
     cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
     e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      rc = batch_launch_raw(ctx, *np, channels, max_n, cap);
+      rc = batch_launch_raw(ctx, *np, max_n, cap);
       cudaGraph_t g = nullptr;
       cudaError_t e2 = cudaStreamEndCapture(cap, &g);
       if (rc == CP_OK && e2 == cudaSuccess) {

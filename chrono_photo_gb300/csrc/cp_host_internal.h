@@ -80,5 +80,12 @@ int ensure_buffer(cp_ctx* ctx, DevBuffer& b, uint64_t bytes);
 int ensure_pinned(cp_ctx* ctx, PinnedBuffer& b, uint64_t bytes);
 bool is_pinned(const void* p);
 void release_plans(cp_ctx* ctx);
+// Batched launches (cp_batch.cpp): the specialised batched kernel a stack takes (index in
+// CP_BATCH_VARIANTS, -1: the general kernel), and one launch over device descriptors.
+int batch_variant_key(const StackDev& d);
+int batch_group_key(const StackDev& d);  // stacks with equal keys share a launch
+int launch_batch_dispatch(cp_ctx* ctx, const std::vector<StackDev>& host, const StackDev* d_stacks,
+                          const int32_t* d_prefix, int32_t total, int32_t interleave,
+                          uint32_t* d_counter, int max_n, cudaStream_t st);
 
 }  // namespace cp

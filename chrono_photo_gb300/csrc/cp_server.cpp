@@ -97,6 +97,7 @@ struct Job {
   uint64_t stage_bytes = 0;
   uint64_t reserved = 0;
   int state = 0;  // 0 queued, 1 admitted (uploading), 2 launched, 3 done
+  int vkey = -1;  // launch group: batched kernel of the job's settings and plane words
   cudaEvent_t staged = nullptr;   // own uploads and the warning-counter reset finished
   cudaEvent_t done_ev = nullptr;
   cp_job_result res{};
@@ -345,23 +346,9 @@ int launch_jobs(cp_server* srv, std::vector<Job*>& batch) {
   uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + nb + 1);
   cudaMemcpyAsync(dp, hp, sizeof(StackDev) * nb + sizeof(int32_t) * (nb + 1),
                   cudaMemcpyHostToDevice, st);
-  cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), st);
-  const int channels = batch[0]->spec.stack.channels;
-  const int smem = smem_bytes_for(max_n, channels);
-  int per_sm = 1;
-  switch (channels) {
-    case 1: per_sm = composite_max_ctas_c1(cta_threads(1), smem); break;
-    case 3: per_sm = composite_max_ctas_c3(cta_threads(3), smem); break;
-    default: per_sm = composite_max_ctas_c4(cta_threads(4), smem); break;
-  }
-  const int grid = std::max(1, std::min(prefix.back(), per_sm * ctx->sm_count));
-  int rc = 0;
-  switch (channels) {
-    case 1: rc = launch_batch_c1(d_stacks, d_prefix, nb, prefix.back(), 0, d_counter, ctx->d_error, grid, smem, st); break;
-    case 3: rc = launch_batch_c3(d_stacks, d_prefix, nb, prefix.back(), 0, d_counter, ctx->d_error, grid, smem, st); break;
-    default: rc = launch_batch_c4(d_stacks, d_prefix, nb, prefix.back(), 0, d_counter, ctx->d_error, grid, smem, st); break;
-  }
-  if (rc) return cuda_status(ctx, static_cast<cudaError_t>(rc), "server launch");
+  const int rc = launch_batch_dispatch(ctx, descs, d_stacks, d_prefix, prefix.back(), 0,
+                                       d_counter, max_n, st);
+  if (rc) return rc;
   cudaEventRecord(slot->ev, st);
   slot->busy = true;
   // results back on the d2h stream once the launch is done
@@ -414,12 +401,13 @@ void worker_loop(cp_server* srv) {
       progressed = true;
     }
     // 2. launch every admitted job whose frames have landed, one launch per channel count
-    std::map<int, std::vector<Job*>> ready;
+    //    and launch group (batched kernel and plane words, see batch_group_key)
+    std::map<std::pair<int, int>, std::vector<Job*>> ready;
     for (Job* j : srv->active) {
       if (j->state != 1) continue;
       const int fr = frames_ready(j);
       if (fr > 0) {
-        ready[j->spec.stack.channels].push_back(j);
+        ready[std::make_pair(j->spec.stack.channels, j->vkey)].push_back(j);
       } else if (fr < 0) {
         cudaGetLastError();
         release(srv, j);
@@ -564,6 +552,7 @@ int cp_server_submit(cp_server* srv, const cp_job* job, uint64_t* job_id) {
     std::vector<const uint8_t*> fr(static_cast<size_t>(s.n), reinterpret_cast<const uint8_t*>(256));
     int rc = prepare_stack(srv->ctx, &j->spec.stack, &j->spec.params, fr.data(), &probe);
     if (rc) return rc;
+    j->vkey = batch_group_key(probe);
   }
   j->res.submit_s = now_s();
   std::lock_guard<std::mutex> lk(srv->mu);
