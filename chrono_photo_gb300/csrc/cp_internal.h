@@ -6,7 +6,6 @@
 
 namespace cp {
 
-constexpr int kPixPerThread = 4;  // a column is 4 pixels = `channels` words per frame row
 constexpr int kTilePx = 128;      // pixels per tile: 32 columns, served by `channels` warps
 inline int cta_threads(int channels) { return 32 * channels; }
 

@@ -1,23 +1,25 @@
-// cp_tile.cuh — frame-stack compositing kernels for sm_103a (included once per channel
-// count by cp_kernels_c*.cu, which instantiate the kernels and their launchers).
+// cp_tile.cuh — frame-stack compositing kernels for sm_103a (included by cp_kernels_c*.cu,
+// which instantiate the general kernels and their launchers, and by cp_kernels_variant.cu /
+// cp_kernels_batch_variant.cu, compiled once per specialised kernel).
 //
-// One CTA processes tiles of `tile_px` consecutive output pixels (4 per thread) across all
-// n frames of a stack:
+// A tile is 128 consecutive output pixels: 32 columns of 4 pixels, i.e. C 32-bit words per
+// column and frame row. A CTA of C warps processes tiles across all n frames of a stack:
 //   1. Warp 0 stages the tile with one cp.async.bulk (TMA engine) per frame row into shared
 //      memory, frame-major, completing on an mbarrier (bounded wait).
-//   2. Each thread owns `C` 32-bit words per frame row (4 pixels x C channels). For every
-//      word it transposes 8 frames x 4 bytes with three delta swaps (8x8 bit transposes)
-//      and a 4x4 byte transpose, giving 8 bit planes of up to 32*NW frames per channel
-//      byte (frame i = bit i).
+//   2. Warp w takes word w of every column (lane = column) and transposes 8 frames x 4
+//      bytes with three delta swaps (8x8 bit transposes) and a 4x4 byte transpose, giving
+//      8 bit planes of up to 32*NW frames per channel byte (frame i = bit i).
 //   3. Order statistics (median, quartiles) come from a radix select on the planes: 8 steps
 //      of popcounts on candidate masks; a pair d[k], d[k+1] takes two passes.
-//   4. Distance pass over all frames: with an abs threshold and 0/1 weights the doubled
-//      distance is exact integer arithmetic, 4*(p-m)^2 = 4*|p-floor m|*|p-ceil m| + [m
-//      half-integer], one dp4a of two vabsdiff4 per pixel and frame; otherwise the f32
-//      terms of src/chrono.rs:261-288 in the reference's operation order.
+//   4. Distance pass, warp w over the frames f = w (mod C), 4 pixels per lane: with an abs
+//      threshold and 0/1 weights the doubled distance is exact integer arithmetic (three
+//      dp4a per pixel and frame); otherwise the f32 terms of src/chrono.rs:261-288 in the
+//      reference's operation order (two pixels per instruction where the ranges allow).
 //   5. Per-pixel epilogue restating src/chrono.rs:290-493: background, outlier pick and
 //      linear blend, the blend mask (src/chrono.rs:183-191) and optional diagnostics.
-// darker/lighter (src/simple.rs:96-133) use the same staging with a streaming fold.
+// Results cross warps through a shared-memory exchange area (Aux). darker/lighter
+// (src/simple.rs:96-133) stream through a TMA stage ring (k_simple_stream), or use the tile
+// staging for cropped / unaligned stacks (simple_tile).
 //
 // Every f32 operation that must round like the Rust reference is an explicit _rn
 // intrinsic, and the library is compiled with -fmad=false: no contraction anywhere.
@@ -36,10 +38,6 @@ namespace {
 #define DEVI __device__ __forceinline__
 
 constexpr long long kWaitCycles = 1ll << 32; // ~2 s at 2 GHz before a wait gives up
-#ifndef CP_DUNROLL
-#define CP_DUNROLL 2
-#endif
-constexpr int kDistUnroll = CP_DUNROLL;        // frames per distance-loop iteration
 
 // ---- PTX wrappers ------------------------------------------------------------------------
 DEVI uint32_t smem_u32(const void* p) {
