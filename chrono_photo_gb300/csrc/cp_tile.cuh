@@ -1277,7 +1277,9 @@ int launch_composite_kind(const StackDev& s, int grid, int smem, void* stream, u
   return static_cast<int>(cudaGetLastError());
 }
 
-// Many stacks: persistent CTAs pull (stack, tile) items from a device counter. A batch whose
+// Many stacks: persistent CTAs pull (stack, tile) items from a device counter.
+constexpr int kBatchPrefixSmem = 65;  // batches of up to 64 stacks search their prefix sums in
+                                      // shared memory (bigger ones in global memory) A batch whose
 // stacks all take one specialised variant (chrono-video windows share their settings) runs
 // that variant; mixed batches the general kernel.
 template <int C, int KIND, int OG, int BG>
@@ -1288,36 +1290,45 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const S
                                                             uint32_t* counter, uint32_t* error) {
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ int item_s, stack_s;
+  __shared__ int32_t prefix_s[kBatchPrefixSmem];  // the tile prefix sums of small batches
   const SmemLayout L = smem_layout(smem);
+  const bool small = n_stacks < kBatchPrefixSmem;
+  if (small && !interleave)
+    for (int i = threadIdx.x; i <= n_stacks; i += blockDim.x) prefix_s[i] = prefix[i];
+  // work item `it` -> (stack_s, item_s); thread 0
+  auto decode = [&](int it) {
+    if (interleave) {
+      // stacks of one geometry (chrono-video windows): tile-major order, so consecutive
+      // items read the same rows of mostly the same frames while they are in L2
+      stack_s = it % n_stacks;
+      item_s = it / n_stacks;
+    } else {
+      const int32_t* pf = small ? prefix_s : prefix;
+      int lo = 0, hi = n_stacks;  // largest s with prefix[s] <= it
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pf[mid] <= it) lo = mid; else hi = mid;
+      }
+      stack_s = lo;
+      item_s = it - pf[lo];
+    }
+    if (it >= total) item_s = -1;
+  };
   if (threadIdx.x == 0) {
     mbar_init(L.bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
+  if (threadIdx.x == 0) decode(static_cast<int>(atomicAdd(counter, 1u)));
+  __syncthreads();
   uint32_t phase = 0;
   int cached = -1;  // stack whose frame bases are in shared memory
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const int it = static_cast<int>(atomicAdd(counter, 1u));
-      if (interleave) {
-        // stacks of one geometry (chrono-video windows): tile-major order, so consecutive
-        // items read the same rows of mostly the same frames while they are in L2
-        stack_s = it % n_stacks;
-        item_s = it / n_stacks;
-      } else {
-        int lo = 0, hi = n_stacks;  // largest s with prefix[s] <= it
-        while (hi - lo > 1) {
-          const int mid = (lo + hi) >> 1;
-          if (prefix[mid] <= it) lo = mid; else hi = mid;
-        }
-        stack_s = lo;
-        item_s = it - prefix[lo];
-      }
-      if (it >= total) item_s = -1;
-    }
-    __syncthreads();
-    const int tile = item_s, s = stack_s;
-    if (tile < 0) break;
+  int tile = item_s, s = stack_s;
+  while (tile >= 0) {
+    // the next item is drawn now and decoded after this tile: the atomic's latency hides
+    // behind the tile's work
+    int next_it = 0;
+    if (threadIdx.x == 0) next_it = static_cast<int>(atomicAdd(counter, 1u));
     const StackDev& S = stacks[s];
     if (s != cached) {
       load_fbase(S, L);
@@ -1327,6 +1338,11 @@ __global__ void __launch_bounds__(32 * C, kMinCtas<C>) k_composite_batch(const S
     uint32_t warn = 0;
     if (!run_tile<C, KIND, OG, BG>(S, tile_geo(S, tile), L, phase, error, warn)) return;
     flush_warnings(S.warnings, warn);
+    // run_tile ended with a barrier: every thread has read item_s / stack_s
+    if (threadIdx.x == 0) decode(next_it);
+    __syncthreads();
+    tile = item_s;
+    s = stack_s;
   }
 }
 
