@@ -201,12 +201,13 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the outlier kernel from the committed ncu summary."""
+def profiled(key):
+    """A per-launch figure (`dram_bytes_per_launch`, `warp_instructions_per_launch`) of the
+    abs/average outlier launch from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_composite_outlier_hd64.md")
     try:
         for line in open(path):
-            if line.strip().startswith("dram_bytes_per_launch:"):
+            if line.strip().startswith(key + ":"):
                 return float(line.split(":")[1].split()[0])
     except Exception:
         pass
@@ -351,7 +352,20 @@ def run_gpu(args):
     peaks, peak_kind = measured_peaks()
     outlier_ms = statistics.mean(per_var[:4])
     achieved = ALGO_BYTES_OUTLIER / (outlier_ms / 1e3) / 1e9
-    traffic = profiled_traffic()
+    traffic = profiled("dram_bytes_per_launch")
+    # the path is bound by instruction issue: the abs/average launch's warp instructions
+    # (ncu) over its CUDA-event time, against 4 issues per clock on every SM
+    instr = profiled("warp_instructions_per_launch")
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    clk_summary = clk.summary()
+    sm_hz = (clk_summary["sm_mhz"] or 2070.0) * 1e6
+    issue_peak = 4.0 * sms * sm_hz / 1e9
+    issue = None
+    if instr:
+        ach = instr / (per_var[0] / 1e3) / 1e9
+        issue = {"achieved": ach, "peak": issue_peak, "unit": "G warp instructions/s",
+                 "frac": ach / issue_peak, "kernel": "k_composite<3, 1, 2, 1> (abs average)",
+                 "instructions_per_launch": instr}
     cpu_v, cpu_dt, cpu_desc = cpu_sample(os.cpu_count() or 1, cpu_band(320), reps=3)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
@@ -365,9 +379,10 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "kernel": "k_composite<3> (outlier)", "peak_kind": peak_kind},
+        "issue_roofline": issue,
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": os.cpu_count(),
                          "kind": "port", "sample": cpu_desc},
-        "clocks": clk.summary(),
+        "clocks": clk_summary,
         "gpu_launches": args.steps * len(VARIANTS),
     }
     print(json.dumps(line), flush=True)
