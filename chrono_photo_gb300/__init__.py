@@ -6,4 +6,5 @@ the reference's processor interface in Python (api.py).
 """
 from ._abi import ChronoError, lib  # noqa: F401
 from .api import (Context, Crop, Fade, OutlierProcessor, Server, ShakeAnalyzer,  # noqa: F401
-                  SimpleProcessor, Threshold, default_context, make_params, video_windows)
+                  SimpleProcessor, Threshold, default_context, load_png, make_params,
+                  png_info, video_windows)

@@ -345,6 +345,35 @@ class ShakeAnalyzer:
         return [tuple(o) for o in ctx.shake_analyze(frames, anchors, anchor_radius, search_radius)]
 
 
+def png_info(path):
+    """(width, height, channels) of a PNG file (cp_png_info)."""
+    w, h, c = ct.c_int32(), ct.c_int32(), ct.c_int32()
+    _check(None, lib().cp_png_info(None, str(path).encode(), ct.byref(w), ct.byref(h),
+                                   ct.byref(c)), "cp_png_info")
+    return w.value, h.value, c.value
+
+
+def load_png(paths, threads=0, out=None, context=None):
+    """Decodes PNG frames (8-bit gray / RGB / RGBA) on `threads` host threads (0: all) into
+    uint8 [n, h, w, c], the layout the compositing entry points take. `out`: optional
+    C-contiguous destination of that shape (e.g. pinned memory); the replacement of the
+    reference's per-frame `image::open` (src/streams.rs:63-70)."""
+    paths = [str(p) for p in paths]
+    if not paths:
+        raise ValueError("no frames")
+    w, h, c = png_info(paths[0])
+    if out is None:
+        out = np.empty((len(paths), h, w, c), np.uint8)
+    if out.shape != (len(paths), h, w, c) or out.dtype != np.uint8 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous uint8 array of shape %s"
+                         % ((len(paths), h, w, c),))
+    arr = (ct.c_char_p * len(paths))(*[p.encode() for p in paths])
+    rc = lib().cp_load_png(context.handle if context else None, arr, len(paths), int(threads),
+                           out.ctypes.data, h * w * c, w, h, c)
+    _check(context.handle if context else None, rc, "cp_load_png")
+    return out
+
+
 def video_windows(image_count, video_in, video_out=(None, None, 1)):
     """chrono-video windows of src/main.rs:230-286: list of (output frame, indices)."""
     (a, b, s), (c, d, t) = video_in, video_out

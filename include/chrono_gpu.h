@@ -44,6 +44,8 @@ extern "C" {
 #define CP_ERR_STATE (-7)   /* object in the wrong state (stopped server, unknown job)     */
 #define CP_ERR_NODEV (-8)   /* no CUDA device with compute capability 10.3                 */
 #define CP_ERR_LIMIT (-9)   /* request above a fixed limit of cp_composite_batch_static    */
+#define CP_ERR_IO (-10)     /* image file missing, unreadable or not a supported PNG       */
+#define CP_ERR_UNSUPPORTED (-11) /* feature not built into this library (no zlib)          */
 
 /* ---- option enums (src/options.rs) --------------------------------------------------- */
 /* SelectionMode, src/options.rs:8-31 */
@@ -249,6 +251,22 @@ int cp_shake_analyze_device(cp_ctx* ctx, const uint8_t* const* frames, int32_t n
                             int32_t width, int32_t height, int32_t channels,
                             const int32_t* anchors, int32_t n_anchors, int32_t anchor_radius,
                             int32_t search_radius, int32_t* offsets, int32_t* diffs);
+
+/* ---- frame ingest ---------------------------------------------------------------------- */
+/* Replaces `image::open(path)` + `as_flat_samples_u8()` of the frame readers
+ * (src/streams.rs:63-70, src/simple.rs:45-52, src/shake.rs:218-255) for PNG files: 8-bit
+ * grayscale (1 channel), RGB (3) or RGBA (4), not interlaced; the decoded samples are the
+ * image's flat u8 layout, row-major, channels interleaved. cp_png_info reads the header of
+ * one file. cp_load_png decodes n files on `threads` host threads (0: all cores) into
+ * out + i * frame_stride (host memory, e.g. from cp_host_alloc, so that cp_composite copies
+ * it to the device at full link speed); every file must have the given width, height and
+ * channels. ctx (nullable) receives the error message. CP_ERR_IO for a missing, truncated,
+ * corrupt or unsupported file; CP_ERR_UNSUPPORTED when the library was built without zlib. */
+int cp_png_info(cp_ctx* ctx, const char* path, int32_t* width, int32_t* height,
+                int32_t* channels);
+int cp_load_png(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t threads,
+                uint8_t* out, uint64_t frame_stride, int32_t width, int32_t height,
+                int32_t channels);
 
 /* ---- serving ------------------------------------------------------------------------- */
 /* A compositing job: a host-memory stack plus options, output buffers in host memory.

@@ -1,0 +1,128 @@
+"""Frame ingest (cp_load_png / cp_png_info): PNG files written here by an independent encoder
+(zlib + the five scanline filters of the PNG specification, chosen per row) must decode to
+exactly the arrays they were written from; unsupported or damaged files fail with
+CP_ERR_IO. CPU only: decoding needs no GPU."""
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+import chrono_photo_gb300 as cg
+from chrono_photo_gb300 import _abi
+
+COLOR_TYPE = {1: 0, 3: 2, 4: 6}
+
+
+def _chunk(kind, body):
+    return struct.pack(">I", len(body)) + kind + body + struct.pack(
+        ">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - c)
+    return np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+
+
+def _filter_rows(img, rng):
+    """Filtered scanlines (filter byte + bytes) with a random filter type per row."""
+    h, w, c = img.shape
+    rows = img.reshape(h, w * c).astype(np.int32)
+    out = bytearray()
+    prev = np.zeros(w * c, np.int32)
+    for y in range(h):
+        x = rows[y]
+        a = np.concatenate([np.zeros(c, np.int32), x[:-c]])
+        b = prev
+        cc = np.concatenate([np.zeros(c, np.int32), prev[:-c]])
+        ft = int(rng.integers(0, 5))
+        pred = [np.zeros_like(x), a, b, (a + b) // 2, _paeth(a, b, cc)][ft]
+        out.append(ft)
+        out += ((x - pred) & 0xFF).astype(np.uint8).tobytes()
+        prev = x
+    return bytes(out)
+
+
+def write_png(path, img, seed=0, level=6, idat_parts=1, text=False, header=None):
+    """img: uint8 [h, w, c]. header: optional (depth, color, interlace) override."""
+    h, w, c = img.shape
+    depth, color, lace = header or (8, COLOR_TYPE[c], 0)
+    data = zlib.compress(_filter_rows(img, np.random.default_rng(seed)), level)
+    parts = np.array_split(np.frombuffer(data, np.uint8), idat_parts)
+    png = b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, color, 0,
+                                                              0, lace))
+    if text:
+        png += _chunk(b"tEXt", b"Comment\x00written by the ingest tests")
+    if color == 3:
+        png += _chunk(b"PLTE", bytes(range(48)))
+    for part in parts:
+        png += _chunk(b"IDAT", part.tobytes())
+    png += _chunk(b"IEND", b"")
+    with open(path, "wb") as f:
+        f.write(png)
+    return path
+
+
+@pytest.mark.parametrize("c", [1, 3, 4])
+@pytest.mark.parametrize("shape", [(1, 1), (3, 5), (21, 37), (64, 200)])
+def test_round_trip(tmp_path, c, shape):
+    rng = np.random.default_rng(shape[0] * 10 + c)
+    n = 5
+    frames = rng.integers(0, 256, size=(n, shape[0], shape[1], c), dtype=np.uint8)
+    paths = [write_png(str(tmp_path / ("f%d.png" % i)), frames[i], seed=i, level=i % 10)
+             for i in range(n)]
+    assert cg.png_info(paths[0]) == (shape[1], shape[0], c)
+    for threads in (1, 3, 0):
+        got = cg.load_png(paths, threads=threads)
+        assert np.array_equal(got, frames)
+
+
+def test_split_data_and_ancillary_chunks(tmp_path):
+    rng = np.random.default_rng(3)
+    img = rng.integers(0, 256, size=(40, 33, 3), dtype=np.uint8)
+    p = write_png(str(tmp_path / "a.png"), img, idat_parts=7, text=True)
+    assert np.array_equal(cg.load_png([p])[0], img)
+
+
+def test_into_preallocated_stack(tmp_path):
+    rng = np.random.default_rng(4)
+    frames = rng.integers(0, 256, size=(3, 9, 11, 4), dtype=np.uint8)
+    paths = [write_png(str(tmp_path / ("g%d.png" % i)), frames[i]) for i in range(3)]
+    out = np.zeros_like(frames)
+    assert cg.load_png(paths, out=out) is out
+    assert np.array_equal(out, frames)
+
+
+def _expect_io(paths):
+    with pytest.raises(cg.ChronoError) as e:
+        cg.load_png(paths)
+    assert e.value.status == _abi.CP_ERR_IO
+
+
+@pytest.mark.parametrize("header", [(8, 2, 1), (16, 2, 0), (8, 3, 0), (8, 4, 0)],
+                         ids=["interlaced", "16-bit", "palette", "gray-alpha"])
+def test_unsupported_formats(tmp_path, header):
+    good = write_png(str(tmp_path / "good.png"), np.zeros((4, 4, 3), np.uint8))
+    bad = write_png(str(tmp_path / "bad.png"), np.zeros((4, 4, 3), np.uint8), header=header)
+    with pytest.raises(cg.ChronoError) as e:
+        cg.png_info(bad)
+    assert e.value.status == _abi.CP_ERR_IO
+    _expect_io([good, bad])
+
+
+def test_damaged_and_mismatched_files(tmp_path):
+    img = np.random.default_rng(5).integers(0, 256, size=(16, 16, 3), dtype=np.uint8)
+    good = write_png(str(tmp_path / "good.png"), img)
+    raw = open(good, "rb").read()
+    trunc = tmp_path / "trunc.png"
+    trunc.write_bytes(raw[:len(raw) // 2])
+    crc = bytearray(raw)
+    crc[40] ^= 0xFF  # inside the IDAT payload: its CRC no longer matches
+    badcrc = tmp_path / "crc.png"
+    badcrc.write_bytes(bytes(crc))
+    other = write_png(str(tmp_path / "other.png"), img[:8])
+    for p in (str(trunc), str(badcrc), str(tmp_path / "missing.png"), other):
+        _expect_io([good, p])
+    with pytest.raises(cg.ChronoError):
+        cg.load_png([str(tmp_path / "missing.png")])
