@@ -20,7 +20,6 @@ CP_ERR_STATE = -7
 CP_ERR_NODEV = -8
 CP_ERR_LIMIT = -9
 CP_ERR_IO = -10
-CP_ERR_UNSUPPORTED = -11
 
 MODE = {"outlier": 0, "darker": 1, "lighter": 2}
 OUTLIER = {"first": 0, "last": 1, "extreme": 2, "average": 3, "forward": 4, "backward": 5}
@@ -129,8 +128,7 @@ STATUS_NAMES = {CP_OK: "ok", CP_ERR_ARG: "invalid argument", CP_ERR_OOM: "out of
                 CP_ERR_TIMEOUT: "timed out", CP_ERR_CUDA: "CUDA error",
                 CP_ERR_BUDGET: "HBM budget exceeded", CP_ERR_RANGE: "out of range",
                 CP_ERR_STATE: "invalid state", CP_ERR_NODEV: "no sm_103 device",
-                CP_ERR_LIMIT: "above a fixed limit", CP_ERR_IO: "image file error",
-                CP_ERR_UNSUPPORTED: "not built into this library"}
+                CP_ERR_LIMIT: "above a fixed limit", CP_ERR_IO: "image file error"}
 
 
 def lib():

@@ -58,18 +58,6 @@ def _run(cmd):
     return p.stdout
 
 
-def _have_zlib(cxx):
-    """PNG ingest needs zlib; without its header and library the ingest entry points build
-    as stubs that return CP_ERR_UNSUPPORTED."""
-    probe = os.path.join(OBJ_DIR, "zlib_probe")
-    src = probe + ".cpp"
-    with open(src, "w") as f:
-        f.write("#include <zlib.h>\nint main() { return zlibVersion() == 0; }\n")
-    p = subprocess.run([cxx, src, "-o", probe, "-lz"], stdout=subprocess.DEVNULL,
-                       stderr=subprocess.DEVNULL)
-    return p.returncode == 0
-
-
 def build(verbose=False, jobs=None):
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
@@ -101,15 +89,12 @@ def build(verbose=False, jobs=None):
             steps.append([nvcc] + ARCH + NVCC_FLAGS + [
                 "-DCP_CH=%d" % ch, "-DCP_KIND=%d" % kind, "-DCP_OG=%d" % og, "-DCP_BG=%d" % bg,
                 "-c", bsrc, "-o", o])
-    zlib = _have_zlib(cxx)
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ_DIR, src + ".o")
         objs.append(o)
         if _stale(o, [s] + hdrs):
-            extra = [] if zlib or src != "cp_ingest.cpp" else ["-DCP_NO_ZLIB"]
-            steps.append([cxx] + CXX_FLAGS + extra + ["-I", os.path.join(cuda, "include"), "-c",
-                                                      s, "-o", o])
+            steps.append([cxx] + CXX_FLAGS + ["-I", os.path.join(cuda, "include"), "-c", s, "-o", o])
     jobs = jobs or max(1, min(len(steps), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         for out in ex.map(_run, steps):
@@ -117,8 +102,7 @@ def build(verbose=False, jobs=None):
                 print(out)
     if steps or not os.path.exists(LIB_PATH):
         tmp = LIB_PATH + ".tmp"
-        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"] +
-             (["-lz"] if zlib else []))
+        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

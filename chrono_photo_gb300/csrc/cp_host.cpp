@@ -471,7 +471,6 @@ const char* cp_status_str(int status) {
     case CP_ERR_NODEV: return "no sm_103 device";
     case CP_ERR_LIMIT: return "request above the fixed limit of the allocation-free entry point";
     case CP_ERR_IO: return "image file missing, unreadable or unsupported";
-    case CP_ERR_UNSUPPORTED: return "not built into this library";
     default: return "unknown status";
   }
 }

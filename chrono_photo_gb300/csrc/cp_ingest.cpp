@@ -4,10 +4,12 @@
 // The reference opens every frame with the `image` crate and takes its flat u8 samples
 // (src/streams.rs:63-70, src/simple.rs:45-52, src/shake.rs:218-255): one decoder call per
 // frame, inside the slicing loop. Here a batch of files is decoded in parallel (one file per
-// task) by a restatement of the PNG format (ISO/IEC 15948): chunk walk with CRC check, zlib
-// inflate of the concatenated IDAT data, and the five scanline filters. PNG is lossless, so
-// the samples are exactly the image's; 8-bit gray, RGB and RGBA without interlacing are
-// accepted (the layouts the compositing kernels take), anything else is CP_ERR_IO.
+// task) by a restatement of the PNG format (ISO/IEC 15948): chunk walk with CRC-32 check,
+// zlib/DEFLATE decoding (RFC 1950/1951) of the concatenated IDAT data with its Adler-32
+// check, and the five scanline filters. The decoder is self-contained (no zlib dependency),
+// so the same code decodes on every host. PNG is lossless, so the samples are exactly the
+// image's; 8-bit gray, RGB and RGBA without interlacing are accepted (the layouts the
+// compositing kernels take), anything else is CP_ERR_IO.
 
 #include <atomic>
 #include <cstdint>
@@ -17,10 +19,6 @@
 #include <string>
 #include <thread>
 #include <vector>
-
-#ifndef CP_NO_ZLIB
-#include <zlib.h>
-#endif
 
 #include "../../include/chrono_gpu.h"
 #include "cp_host_internal.h"
@@ -46,6 +44,363 @@ bool read_file(const char* path, std::vector<uint8_t>* data) {
   const bool ok = !std::ferror(f);
   std::fclose(f);
   return ok;
+}
+
+// ---- CRC-32 of the PNG chunks (ISO 3309 polynomial, reflected 0xEDB88320), slice-by-8 ----
+
+struct CrcTables {
+  uint32_t t[8][256];
+  CrcTables() {
+    for (uint32_t i = 0; i < 256; ++i) {
+      uint32_t c = i;
+      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      t[0][i] = c;
+    }
+    for (int s = 1; s < 8; ++s)
+      for (uint32_t i = 0; i < 256; ++i) t[s][i] = (t[s - 1][i] >> 8) ^ t[0][t[s - 1][i] & 0xFF];
+  }
+};
+
+uint32_t crc32_png(const uint8_t* p, size_t n) {
+  static const CrcTables T;
+  uint32_t c = 0xFFFFFFFFu;
+  while (n >= 8) {
+    const uint32_t lo = c ^ (p[0] | (p[1] << 8) | (p[2] << 16) | (static_cast<uint32_t>(p[3]) << 24));
+    const uint32_t hi = p[4] | (p[5] << 8) | (p[6] << 16) | (static_cast<uint32_t>(p[7]) << 24);
+    c = T.t[7][lo & 0xFF] ^ T.t[6][(lo >> 8) & 0xFF] ^ T.t[5][(lo >> 16) & 0xFF] ^ T.t[4][lo >> 24] ^
+        T.t[3][hi & 0xFF] ^ T.t[2][(hi >> 8) & 0xFF] ^ T.t[1][(hi >> 16) & 0xFF] ^ T.t[0][hi >> 24];
+    p += 8;
+    n -= 8;
+  }
+  while (n--) c = T.t[0][(c ^ *p++) & 0xFF] ^ (c >> 8);
+  return c ^ 0xFFFFFFFFu;
+}
+
+// ---- Adler-32 of the zlib stream's decompressed data (RFC 1950 section 9) ----
+
+uint32_t adler32(const uint8_t* p, size_t n) {
+  uint32_t a = 1, b = 0;
+  while (n > 0) {
+    // 5552 is the largest run for which b cannot overflow 32 bits before the reduction.
+    size_t run = n < 5552 ? n : 5552;
+    n -= run;
+    while (run--) {
+      a += *p++;
+      b += a;
+    }
+    a %= 65521u;
+    b %= 65521u;
+  }
+  return (b << 16) | a;
+}
+
+// ---- DEFLATE decoder (RFC 1951) writing into a buffer of known size ----
+
+// Canonical Huffman code: symbols sorted by code length; `fast` maps the next kFast input
+// bits (least significant first, as DEFLATE packs codes bit-reversed) to symbol << 4 | length
+// for codes of at most kFast bits, 0 for longer codes, which the canonical walk decodes.
+constexpr int kFast = 10;
+constexpr int kMaxBits = 15;
+
+struct Huffman {
+  uint16_t count[kMaxBits + 1];
+  uint16_t symbol[288];
+  uint16_t fast[1 << kFast];
+};
+
+// Builds `h` from per-symbol code lengths. False when the lengths over-subscribe the code
+// space; incomplete codes are accepted (an unassigned code then fails at decode time).
+bool build_huffman(Huffman* h, const uint8_t* lengths, int n) {
+  std::memset(h->count, 0, sizeof h->count);
+  for (int s = 0; s < n; ++s) h->count[lengths[s]]++;
+  h->count[0] = 0;
+  int left = 1;
+  for (int len = 1; len <= kMaxBits; ++len) {
+    left = (left << 1) - h->count[len];
+    if (left < 0) return false;
+  }
+  uint16_t offs[kMaxBits + 2];
+  offs[1] = 0;
+  for (int len = 1; len <= kMaxBits; ++len) offs[len + 1] = offs[len] + h->count[len];
+  for (int s = 0; s < n; ++s)
+    if (lengths[s]) h->symbol[offs[lengths[s]]++] = static_cast<uint16_t>(s);
+  std::memset(h->fast, 0, sizeof h->fast);
+  uint32_t code = 0;
+  int idx = 0;
+  for (int len = 1; len <= kFast; ++len) {
+    for (int k = 0; k < h->count[len]; ++k, ++idx, ++code) {
+      uint32_t rev = 0;
+      for (int b = 0; b < len; ++b) rev |= ((code >> b) & 1u) << (len - 1 - b);
+      const uint16_t e = static_cast<uint16_t>((h->symbol[idx] << 4) | len);
+      for (uint32_t fill = rev; fill < (1u << kFast); fill += 1u << len) h->fast[fill] = e;
+    }
+    code <<= 1;
+  }
+  return true;
+}
+
+class Inflater {
+ public:
+  Inflater(const uint8_t* in, size_t n_in, uint8_t* out, size_t n_out)
+      : in_(in), n_in_(n_in), out_(out), n_out_(n_out) {}
+
+  // Decodes the whole DEFLATE stream; on success `consumed()` is the number of input bytes
+  // it occupied (rounded up to a byte) and `produced()` the output length.
+  bool run(std::string* why) {
+    bool last = false;
+    while (!last) {
+      last = bits(1) != 0;
+      const uint32_t type = bits(2);
+      bool ok;
+      if (type == 0) ok = stored(why);
+      else if (type == 1) ok = fixed(why);
+      else if (type == 2) ok = dynamic(why);
+      else {
+        *why = "bad DEFLATE block type";
+        ok = false;
+      }
+      if (!ok) return false;
+      if (overrun()) {
+        *why = "truncated image data";
+        return false;
+      }
+    }
+    return true;
+  }
+  size_t produced() const { return pos_out_; }
+  size_t consumed() const { return pos_in_ - nbits_ / 8; }
+
+ private:
+  void refill() {
+    while (nbits_ <= 56) {
+      const uint64_t byte = pos_in_ < n_in_ ? in_[pos_in_] : 0;  // zeros past the end
+      ++pos_in_;
+      buf_ |= byte << nbits_;
+      nbits_ += 8;
+    }
+  }
+  bool overrun() const { return pos_in_ - nbits_ / 8 > n_in_; }
+  uint32_t bits(int n) {
+    if (nbits_ < n) refill();
+    const uint32_t v = static_cast<uint32_t>(buf_ & ((1ull << n) - 1));
+    buf_ >>= n;
+    nbits_ -= n;
+    return v;
+  }
+
+  // Next symbol of `h`, or -1 for a code that the table does not assign.
+  int decode(const Huffman& h) {
+    if (nbits_ < kMaxBits) refill();
+    const uint16_t e = h.fast[buf_ & ((1u << kFast) - 1)];
+    if (e) {
+      buf_ >>= e & 15;
+      nbits_ -= e & 15;
+      return e >> 4;
+    }
+    // Canonical walk: codes of each length are consecutive integers starting at `first`.
+    int code = 0, first = 0, index = 0;
+    for (int len = 1; len <= kMaxBits; ++len) {
+      code |= static_cast<int>((buf_ >> (len - 1)) & 1);
+      const int count = h.count[len];
+      if (code - first < count) {
+        buf_ >>= len;
+        nbits_ -= len;
+        return h.symbol[index + code - first];
+      }
+      index += count;
+      first = (first + count) << 1;
+      code <<= 1;
+    }
+    return -1;
+  }
+
+  bool stored(std::string* why) {
+    // Drop the bits up to the next byte boundary, then return whole unread bytes to the input.
+    buf_ >>= nbits_ & 7;
+    nbits_ -= nbits_ & 7;
+    pos_in_ -= nbits_ / 8;
+    buf_ = 0;
+    nbits_ = 0;
+    if (pos_in_ + 4 > n_in_) {
+      *why = "truncated image data";
+      return false;
+    }
+    const uint32_t len = in_[pos_in_] | (in_[pos_in_ + 1] << 8);
+    const uint32_t nlen = in_[pos_in_ + 2] | (in_[pos_in_ + 3] << 8);
+    pos_in_ += 4;
+    if ((len ^ 0xFFFFu) != nlen) {
+      *why = "bad stored block length";
+      return false;
+    }
+    if (pos_in_ + len > n_in_ || pos_out_ + len > n_out_) {
+      *why = pos_in_ + len > n_in_ ? "truncated image data" : "image data longer than the image";
+      return false;
+    }
+    std::memcpy(out_ + pos_out_, in_ + pos_in_, len);
+    pos_in_ += len;
+    pos_out_ += len;
+    return true;
+  }
+
+  bool fixed(std::string* why) {
+    static const struct Fixed {
+      Huffman lit, dist;
+      Fixed() {
+        uint8_t l[288];
+        for (int s = 0; s < 288; ++s) l[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
+        build_huffman(&lit, l, 288);
+        uint8_t d[30];
+        std::memset(d, 5, sizeof d);
+        build_huffman(&dist, d, 30);
+      }
+    } F;
+    return codes(F.lit, F.dist, why);
+  }
+
+  bool dynamic(std::string* why) {
+    static const uint8_t kOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+    const int nlen = static_cast<int>(bits(5)) + 257;
+    const int ndist = static_cast<int>(bits(5)) + 1;
+    const int ncode = static_cast<int>(bits(4)) + 4;
+    if (nlen > 286 || ndist > 30) {
+      *why = "bad dynamic block header";
+      return false;
+    }
+    uint8_t lengths[320];
+    std::memset(lengths, 0, 19);
+    for (int i = 0; i < ncode; ++i) lengths[kOrder[i]] = static_cast<uint8_t>(bits(3));
+    Huffman lencode;
+    if (!build_huffman(&lencode, lengths, 19)) {
+      *why = "bad code-length code";
+      return false;
+    }
+    int i = 0;
+    while (i < nlen + ndist) {
+      const int sym = decode(lencode);
+      if (sym < 0) {
+        *why = "bad code-length code";
+        return false;
+      }
+      if (sym < 16) {
+        lengths[i++] = static_cast<uint8_t>(sym);
+        continue;
+      }
+      int rep;
+      uint8_t val = 0;
+      if (sym == 16) {
+        if (i == 0) {
+          *why = "repeat without a previous length";
+          return false;
+        }
+        val = lengths[i - 1];
+        rep = 3 + static_cast<int>(bits(2));
+      } else if (sym == 17) {
+        rep = 3 + static_cast<int>(bits(3));
+      } else {
+        rep = 11 + static_cast<int>(bits(7));
+      }
+      if (i + rep > nlen + ndist) {
+        *why = "code lengths overflow";
+        return false;
+      }
+      while (rep--) lengths[i++] = val;
+    }
+    if (lengths[256] == 0) {
+      *why = "no end-of-block code";
+      return false;
+    }
+    Huffman lit, dist;
+    if (!build_huffman(&lit, lengths, nlen) || !build_huffman(&dist, lengths + nlen, ndist)) {
+      *why = "over-subscribed Huffman code";
+      return false;
+    }
+    return codes(lit, dist, why);
+  }
+
+  // Literal/length + distance symbols of one compressed block, up to end-of-block (256).
+  bool codes(const Huffman& lit, const Huffman& dist, std::string* why) {
+    static const uint16_t kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27,
+                                          31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+    static const uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                          2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+    static const uint16_t kDistBase[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129,
+                                           193, 257, 385, 513, 769, 1025, 1537, 2049, 3073,
+                                           4097, 6145, 8193, 12289, 16385, 24577};
+    static const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
+                                           6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+    for (;;) {
+      const int sym = decode(lit);
+      if (sym < 256) {
+        if (sym < 0) {
+          *why = "bad literal/length code";
+          return false;
+        }
+        if (pos_out_ >= n_out_) {
+          *why = "image data longer than the image";
+          return false;
+        }
+        out_[pos_out_++] = static_cast<uint8_t>(sym);
+        continue;
+      }
+      if (sym == 256) return true;
+      if (sym > 285) {
+        *why = "bad length symbol";
+        return false;
+      }
+      const size_t len = kLenBase[sym - 257] + bits(kLenExtra[sym - 257]);
+      const int dsym = decode(dist);
+      if (dsym < 0 || dsym > 29) {
+        *why = "bad distance code";
+        return false;
+      }
+      const size_t d = kDistBase[dsym] + bits(kDistExtra[dsym]);
+      if (d > pos_out_ || len > n_out_ - pos_out_) {
+        *why = d > pos_out_ ? "distance before the start of the data" : "image data longer than the image";
+        return false;
+      }
+      uint8_t* dst = out_ + pos_out_;
+      const uint8_t* src = dst - d;
+      if (d >= len) {
+        std::memcpy(dst, src, len);
+      } else {
+        for (size_t k = 0; k < len; ++k) dst[k] = src[k];  // overlapping copy repeats the run
+      }
+      pos_out_ += len;
+      if (overrun()) {
+        *why = "truncated image data";
+        return false;
+      }
+    }
+  }
+
+  const uint8_t* in_;
+  size_t n_in_, pos_in_ = 0;
+  uint8_t* out_;
+  size_t n_out_, pos_out_ = 0;
+  uint64_t buf_ = 0;
+  int nbits_ = 0;
+};
+
+// Decompresses a zlib stream (RFC 1950: header, DEFLATE data, Adler-32 of the output) into
+// exactly `n_out` bytes.
+bool zlib_decode(const uint8_t* in, size_t n_in, uint8_t* out, size_t n_out, std::string* why) {
+  if (n_in < 6 || (in[0] & 15) != 8 || (in[0] >> 4) > 7 || ((in[0] << 8) | in[1]) % 31 != 0 ||
+      (in[1] & 0x20)) {
+    *why = "bad zlib header";
+    return false;
+  }
+  Inflater inf(in + 2, n_in - 2, out, n_out);
+  if (!inf.run(why)) return false;
+  if (inf.produced() != n_out) {
+    *why = "image data shorter than the image";
+    return false;
+  }
+  const size_t tail = 2 + inf.consumed();
+  if (tail + 4 > n_in || be32(in + tail) != adler32(out, n_out)) {
+    *why = tail + 4 > n_in ? "truncated image data" : "Adler-32 mismatch";
+    return false;
+  }
+  return true;
 }
 
 // The Paeth predictor of the PNG specification (filter type 4).
@@ -124,13 +479,10 @@ int parse_png(const std::vector<uint8_t>& d, PngHeader* h, std::vector<uint8_t>*
       return CP_ERR_IO;
     }
     const uint8_t* body = &d[pos + 8];
-#ifndef CP_NO_ZLIB
-    const uLong crc = crc32(crc32(0L, Z_NULL, 0), type, 4 + len);
-    if (crc != be32(body + len)) {
+    if (crc32_png(type, 4 + len) != be32(body + len)) {
       *why = "chunk CRC mismatch";
       return CP_ERR_IO;
     }
-#endif
     if (std::memcmp(type, "IHDR", 4) == 0) {
       if (len != 13 || have_header) {
         *why = "bad IHDR";
@@ -181,11 +533,6 @@ struct Scratch {
 // Decodes one file into `out` (height rows of width * channels bytes).
 int decode_png(const char* path, const PngHeader& want, uint8_t* out, Scratch* s,
                std::string* why) {
-#ifdef CP_NO_ZLIB
-  (void)path; (void)want; (void)out; (void)s;
-  *why = "built without zlib";
-  return CP_ERR_UNSUPPORTED;
-#else
   if (!read_file(path, &s->file)) {
     *why = std::string("cannot read ") + path;
     return CP_ERR_IO;
@@ -203,10 +550,8 @@ int decode_png(const char* path, const PngHeader& want, uint8_t* out, Scratch* s
   const size_t stride = static_cast<size_t>(h.width) * h.channels;
   const size_t need = static_cast<size_t>(h.height) * (stride + 1);
   s->raw.resize(need);
-  uLongf got = static_cast<uLongf>(need);
-  if (uncompress(s->raw.data(), &got, s->idat.data(), static_cast<uLong>(s->idat.size())) != Z_OK ||
-      got != need) {
-    *why = std::string(path) + ": corrupt image data";
+  if (!zlib_decode(s->idat.data(), s->idat.size(), s->raw.data(), need, why)) {
+    *why = std::string(path) + ": " + *why;
     return CP_ERR_IO;
   }
   if (!unfilter(s->raw.data(), h.height, stride, h.channels, out)) {
@@ -214,7 +559,6 @@ int decode_png(const char* path, const PngHeader& want, uint8_t* out, Scratch* s
     return CP_ERR_IO;
   }
   return CP_OK;
-#endif
 }
 
 }  // namespace

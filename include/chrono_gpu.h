@@ -45,7 +45,6 @@ extern "C" {
 #define CP_ERR_NODEV (-8)   /* no CUDA device with compute capability 10.3                 */
 #define CP_ERR_LIMIT (-9)   /* request above a fixed limit of cp_composite_batch_static    */
 #define CP_ERR_IO (-10)     /* image file missing, unreadable or not a supported PNG       */
-#define CP_ERR_UNSUPPORTED (-11) /* feature not built into this library (no zlib)          */
 
 /* ---- option enums (src/options.rs) --------------------------------------------------- */
 /* SelectionMode, src/options.rs:8-31 */
@@ -261,7 +260,7 @@ int cp_shake_analyze_device(cp_ctx* ctx, const uint8_t* const* frames, int32_t n
  * out + i * frame_stride (host memory, e.g. from cp_host_alloc, so that cp_composite copies
  * it to the device at full link speed); every file must have the given width, height and
  * channels. ctx (nullable) receives the error message. CP_ERR_IO for a missing, truncated,
- * corrupt or unsupported file; CP_ERR_UNSUPPORTED when the library was built without zlib. */
+ * corrupt (chunk CRC-32, zlib Adler-32 or DEFLATE data) or unsupported file. */
 int cp_png_info(cp_ctx* ctx, const char* path, int32_t* width, int32_t* height,
                 int32_t* channels);
 int cp_load_png(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t threads,

@@ -44,11 +44,25 @@ def _filter_rows(img, rng):
     return bytes(out)
 
 
-def write_png(path, img, seed=0, level=6, idat_parts=1, text=False, header=None):
-    """img: uint8 [h, w, c]. header: optional (depth, color, interlace) override."""
+def _deflate(raw, level, strategy):
+    z = zlib.compressobj(level, zlib.DEFLATED, 15, 9, strategy)
+    return z.compress(raw) + z.flush()
+
+
+def write_png(path, img, seed=0, level=6, idat_parts=1, text=False, header=None,
+              strategy=zlib.Z_DEFAULT_STRATEGY, filters=True, damage=None):
+    """img: uint8 [h, w, c]. header: optional (depth, color, interlace) override.
+    filters=False writes every row with filter type 0; damage(data) may alter the zlib
+    stream before it is split into IDAT chunks (with valid chunk CRCs)."""
     h, w, c = img.shape
     depth, color, lace = header or (8, COLOR_TYPE[c], 0)
-    data = zlib.compress(_filter_rows(img, np.random.default_rng(seed)), level)
+    if filters:
+        raw = _filter_rows(img, np.random.default_rng(seed))
+    else:
+        raw = np.concatenate([np.zeros((h, 1), np.uint8), img.reshape(h, w * c)], 1).tobytes()
+    data = _deflate(raw, level, strategy)
+    if damage:
+        data = damage(data)
     parts = np.array_split(np.frombuffer(data, np.uint8), idat_parts)
     png = b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, color, 0,
                                                               0, lace))
@@ -76,6 +90,41 @@ def test_round_trip(tmp_path, c, shape):
     for threads in (1, 3, 0):
         got = cg.load_png(paths, threads=threads)
         assert np.array_equal(got, frames)
+
+
+def _photo_like(h, w, c, seed):
+    """Smooth gradients with a little noise and repeated patches: compresses with many
+    back-references, as camera frames do."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w]
+    base = np.stack([(x * (k + 1) + y * (3 - k)) // 4 for k in range(c)], -1)
+    img = (base + rng.integers(0, 3, size=(h, w, c))) % 256
+    k = min(8, h - h // 3)
+    img[h // 3: h // 3 + k] = img[:k]
+    return img.astype(np.uint8)
+
+
+@pytest.mark.parametrize("strategy", [zlib.Z_DEFAULT_STRATEGY, zlib.Z_FILTERED,
+                                      zlib.Z_HUFFMAN_ONLY, zlib.Z_RLE, zlib.Z_FIXED],
+                         ids=["default", "filtered", "huffman-only", "rle", "fixed"])
+@pytest.mark.parametrize("level", [1, 6, 9])
+def test_deflate_block_kinds(tmp_path, strategy, level):
+    """Dynamic and fixed Huffman blocks, short and long matches, overlapping runs."""
+    frames = np.stack([_photo_like(48, 300, 3, s) for s in range(3)])
+    paths = [write_png(str(tmp_path / ("d%d.png" % i)), frames[i], seed=i, level=level,
+                       strategy=strategy, filters=i != 1) for i in range(3)]
+    assert np.array_equal(cg.load_png(paths, threads=2), frames)
+
+
+def test_long_distance_and_stored_blocks(tmp_path):
+    """Rows of 24000 bytes repeated: matches reach back ~24 KB (the distance codes with the
+    most extra bits); level 0 gives stored blocks of up to 64 KB, several per image."""
+    row = np.random.default_rng(9).integers(0, 256, size=(1, 8000, 3), dtype=np.uint8)
+    img = np.repeat(row, 6, 0)
+    img[3, 100:200] ^= 0x5A
+    for level in (0, 9):
+        p = write_png(str(tmp_path / ("l%d.png" % level)), img, level=level, filters=False)
+        assert np.array_equal(cg.load_png([p])[0], img)
 
 
 def test_split_data_and_ancillary_chunks(tmp_path):
@@ -124,5 +173,36 @@ def test_damaged_and_mismatched_files(tmp_path):
     other = write_png(str(tmp_path / "other.png"), img[:8])
     for p in (str(trunc), str(badcrc), str(tmp_path / "missing.png"), other):
         _expect_io([good, p])
+
+
+def _flip(i, mask=0x01):
+    def damage(d):
+        d = bytearray(d)
+        d[i] ^= mask
+        return bytes(d)
+    return damage
+
+
+@pytest.mark.parametrize("damage", [
+    _flip(-1),                                     # Adler-32 of the data
+    _flip(0, 0x07),                                # zlib header: compression method
+    _flip(1, 0x20),                                # zlib header: preset dictionary flag
+    lambda d: d[:-9],                              # DEFLATE stream cut short
+    lambda d: d[:2] + bytes([0x07]) + d[3:],       # final block of reserved type 3
+], ids=["adler", "method", "dictionary", "cut", "block-type"])
+def test_damaged_zlib_stream(tmp_path, damage):
+    """Chunk CRCs are valid here: the zlib layer itself must catch each defect."""
+    img = _photo_like(24, 50, 3, 1)
+    good = write_png(str(tmp_path / "good.png"), img, level=9)
+    bad = write_png(str(tmp_path / "bad.png"), img, level=9, damage=damage)
+    _expect_io([good, bad])
+
+
+def test_image_data_longer_than_the_image(tmp_path):
+    img = _photo_like(8, 10, 3, 2)
+    bigger = _photo_like(9, 10, 3, 2)
+    raw = np.concatenate([np.zeros((9, 1), np.uint8), bigger.reshape(9, 30)], 1).tobytes()
+    p = write_png(str(tmp_path / "x.png"), img, damage=lambda d: zlib.compress(raw))
+    _expect_io([p])
     with pytest.raises(cg.ChronoError):
         cg.load_png([str(tmp_path / "missing.png")])
