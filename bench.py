@@ -745,13 +745,88 @@ def run_shake(args):
         "clocks": clk.summary()}), flush=True)
 
 
+def run_ingest(args):
+    """Frame ingest: the HD stack written as 64 PNG files (Paeth-filtered, zlib level 6),
+    decoded by cp_load_png on all host threads into pinned memory, then composited from there
+    by cp_composite (abs/0.05/0.2 average): files -> composite, the work the reference does
+    per frame inside its slicing loop (src/streams.rs:63-70). Also reports one-thread decode,
+    the reference's per-frame sequential decode rate."""
+    import shutil
+    import tempfile
+    import numpy as np
+    from chrono_photo_gb300 import example_data, make_params
+    ctx, lib, _abi, local = _ctx_and_lib()
+    fb = W * H * C
+    frames = example_data.hd_stack(seed=2)
+    tmp = tempfile.mkdtemp(prefix="cp_ingest_")
+    try:
+        threads = os.cpu_count() or 1
+        paths = example_data.write_pngs(frames, tmp, level=6, threads=threads)
+        file_bytes = sum(os.path.getsize(p) for p in paths)
+        hptr, host = _pinned(ctx, lib, N_FRAMES * fb)
+        host = host.reshape(N_FRAMES, H, W, C)
+        arr = (ct.c_char_p * N_FRAMES)(*[p.encode() for p in paths])
+
+        def decode(nthreads, n=N_FRAMES):
+            ctx.check(lib.cp_load_png(ctx.handle, arr, n, nthreads, hptr, fb, W, H, C),
+                      "cp_load_png")
+        decode(threads)
+        exact = bool(np.array_equal(host, frames))
+        keep = []
+        p = make_params(keep=keep, mode="outlier", threshold="abs/0.05/0.2", outlier="average",
+                        background="first")
+        stack = _abi.Stack(n=N_FRAMES, width=W, height=H, channels=C, base=hptr,
+                           frame_stride=fb)
+        optr, _ = _pinned(ctx, lib, 2 * fb)
+
+        def composite():
+            ctx.check(lib.cp_composite(ctx.handle, ct.byref(stack), ct.byref(p), optr,
+                                       optr + fb, None, None), "cp_composite")
+        composite()
+        steps = max(1, min(args.steps, 5))
+        t_dec = t_comp = 0.0
+        with ClockSampler(local) as clk:
+            for _ in range(steps):
+                t0 = time.perf_counter()
+                decode(threads)
+                t1 = time.perf_counter()
+                composite()
+                t2 = time.perf_counter()
+                t_dec += t1 - t0
+                t_comp += t2 - t1
+        t_dec /= steps
+        t_comp /= steps
+        n1 = 8
+        decode(1, n1)
+        t0 = time.perf_counter()
+        decode(1, n1)
+        t_one = (time.perf_counter() - t0) / n1
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    print(json.dumps({
+        "workload": "ingest", "metric": "frames/s", "value": N_FRAMES / t_dec, "unit": "frames/s",
+        "threads": threads, "decoded_exact": exact,
+        "decode_ms_per_stack": 1e3 * t_dec, "decoded_MB_per_s": N_FRAMES * fb / t_dec / 1e6,
+        "one_thread_frames_per_s": 1.0 / t_one,
+        "files_to_composite": {"value": MPXF_PER_COMPOSITE / (t_dec + t_comp), "unit": METRIC,
+                               "decode_ms": 1e3 * t_dec, "composite_e2e_ms": 1e3 * t_comp,
+                               "note": "decode, then cp_composite from pinned memory (H2D, "
+                                       "kernel, D2H of composite and mask)"},
+        "steps": steps, "dtype": "u8", "data": "synthetic (seeded HD stack written as PNG)",
+        "config": {"frames": N_FRAMES, "width": W, "height": H, "channels": C,
+                   "png": "8-bit RGB, Paeth filter, zlib level 6",
+                   "compressed_MB_per_frame": file_bytes / N_FRAMES / 1e6},
+        "clocks": clk.summary()}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hd", choices=["hd", "video", "serve", "shake"],
+    ap.add_argument("--workload", default="hd",
+                    choices=["hd", "video", "serve", "shake", "ingest"],
                     help="hd (default): the headline line; the others print their own lines")
     ap.add_argument("--jobs", type=int, default=512, help="serve: number of jobs")
     args = ap.parse_args()
@@ -769,6 +844,8 @@ def main():
             run_serve(args)
         elif args.workload == "shake":
             run_shake(args)
+        elif args.workload == "ingest":
+            run_ingest(args)
         else:
             run_gpu(args)
     finally:

@@ -99,7 +99,7 @@ uint32_t adler32(const uint8_t* p, size_t n) {
 // Canonical Huffman code: symbols sorted by code length; `fast` maps the next kFast input
 // bits (least significant first, as DEFLATE packs codes bit-reversed) to symbol << 4 | length
 // for codes of at most kFast bits, 0 for longer codes, which the canonical walk decodes.
-constexpr int kFast = 10;
+constexpr int kFast = 11;
 constexpr int kMaxBits = 15;
 
 struct Huffman {
@@ -139,6 +139,10 @@ bool build_huffman(Huffman* h, const uint8_t* lengths, int n) {
   return true;
 }
 
+// Bytes that the decoder may write past the end of its output (match copies move 8-byte
+// words); the output buffer must have this many writable bytes after n_out.
+constexpr size_t kCopySlack = 16;
+
 class Inflater {
  public:
   Inflater(const uint8_t* in, size_t n_in, uint8_t* out, size_t n_out)
@@ -171,7 +175,20 @@ class Inflater {
   size_t consumed() const { return pos_in_ - nbits_ / 8; }
 
  private:
+  // Tops the bit buffer up to at least 56 bits. Away from the end of the input, one
+  // unaligned 8-byte little-endian load: whole bytes are consumed, and the bits above
+  // nbits_ that the load also sets are the same input bits the next load ORs in again.
   void refill() {
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+    if (pos_in_ + 8 <= n_in_) {
+      uint64_t v;
+      std::memcpy(&v, in_ + pos_in_, 8);
+      buf_ |= v << nbits_;
+      pos_in_ += (63 - nbits_) >> 3;
+      nbits_ |= 56;
+      return;
+    }
+#endif
     while (nbits_ <= 56) {
       const uint64_t byte = pos_in_ < n_in_ ? in_[pos_in_] : 0;  // zeros past the end
       ++pos_in_;
@@ -182,6 +199,9 @@ class Inflater {
   bool overrun() const { return pos_in_ - nbits_ / 8 > n_in_; }
   uint32_t bits(int n) {
     if (nbits_ < n) refill();
+    return bits_buffered(n);
+  }
+  uint32_t bits_buffered(int n) {
     const uint32_t v = static_cast<uint32_t>(buf_ & ((1ull << n) - 1));
     buf_ >>= n;
     nbits_ -= n;
@@ -191,6 +211,10 @@ class Inflater {
   // Next symbol of `h`, or -1 for a code that the table does not assign.
   int decode(const Huffman& h) {
     if (nbits_ < kMaxBits) refill();
+    return decode_buffered(h);
+  }
+  // decode() with at least kMaxBits bits already in the buffer.
+  int decode_buffered(const Huffman& h) {
     const uint16_t e = h.fast[buf_ & ((1u << kFast) - 1)];
     if (e) {
       buf_ >>= e & 15;
@@ -329,7 +353,9 @@ class Inflater {
     static const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
                                            6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
     for (;;) {
-      const int sym = decode(lit);
+      // One symbol with its match takes at most 15 + 5 + 15 + 13 = 48 bits.
+      if (nbits_ < 48) refill();
+      const int sym = decode_buffered(lit);
       if (sym < 256) {
         if (sym < 0) {
           *why = "bad literal/length code";
@@ -347,21 +373,30 @@ class Inflater {
         *why = "bad length symbol";
         return false;
       }
-      const size_t len = kLenBase[sym - 257] + bits(kLenExtra[sym - 257]);
-      const int dsym = decode(dist);
+      const size_t len = kLenBase[sym - 257] + bits_buffered(kLenExtra[sym - 257]);
+      const int dsym = decode_buffered(dist);
       if (dsym < 0 || dsym > 29) {
         *why = "bad distance code";
         return false;
       }
-      const size_t d = kDistBase[dsym] + bits(kDistExtra[dsym]);
+      const size_t d = kDistBase[dsym] + bits_buffered(kDistExtra[dsym]);
       if (d > pos_out_ || len > n_out_ - pos_out_) {
         *why = d > pos_out_ ? "distance before the start of the data" : "image data longer than the image";
         return false;
       }
       uint8_t* dst = out_ + pos_out_;
       const uint8_t* src = dst - d;
-      if (d >= len) {
-        std::memcpy(dst, src, len);
+      if (d >= 8) {
+        // 8-byte words, each read from bytes already final (d >= 8); the last word may
+        // run up to 7 bytes past the match, into bytes written later or the slack.
+        uint8_t* const end = dst + len;
+        do {
+          uint64_t w;
+          std::memcpy(&w, src, 8);
+          std::memcpy(dst, &w, 8);
+          src += 8;
+          dst += 8;
+        } while (dst < end);
       } else {
         for (size_t k = 0; k < len; ++k) dst[k] = src[k];  // overlapping copy repeats the run
       }
@@ -382,7 +417,7 @@ class Inflater {
 };
 
 // Decompresses a zlib stream (RFC 1950: header, DEFLATE data, Adler-32 of the output) into
-// exactly `n_out` bytes.
+// exactly `n_out` bytes; `out` has kCopySlack writable bytes beyond them.
 bool zlib_decode(const uint8_t* in, size_t n_in, uint8_t* out, size_t n_out, std::string* why) {
   if (n_in < 6 || (in[0] & 15) != 8 || (in[0] >> 4) > 7 || ((in[0] << 8) | in[1]) % 31 != 0 ||
       (in[1] & 0x20)) {
@@ -403,56 +438,71 @@ bool zlib_decode(const uint8_t* in, size_t n_in, uint8_t* out, size_t n_out, std
   return true;
 }
 
-// The Paeth predictor of the PNG specification (filter type 4).
-inline uint8_t paeth(int a, int b, int c) {
-  const int p = a + b - c;
-  const int pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
-  if (pa <= pb && pa <= pc) return static_cast<uint8_t>(a);
-  if (pb <= pc) return static_cast<uint8_t>(b);
-  return static_cast<uint8_t>(c);
+// The Paeth predictor of the PNG specification (filter type 4): of a (left), b (above) and
+// c (upper left), the one nearest to a + b - c, ties in the order a, b, c. Written with
+// selects rather than branches: on noisy images the choice is unpredictable.
+inline int paeth(int a, int b, int c) {
+  const int pa = std::abs(b - c), pb = std::abs(a - c), pc = std::abs(a + b - 2 * c);
+  const int bc = pb <= pc ? b : c;
+  return ((pa <= pb) & (pa <= pc)) ? a : bc;
 }
 
 // Reverses the per-scanline filters of `raw` (height rows of 1 + stride bytes) into `out`
-// (rows of `stride` bytes); bpp = bytes per pixel. False on an unknown filter type.
-bool unfilter(const uint8_t* raw, int32_t height, size_t stride, int bpp, uint8_t* out) {
-  const uint8_t* prev = nullptr;
+// (rows of `stride` bytes) for BPP bytes per pixel. The row above the first is zero, as is
+// the pixel left of the first. False on an unknown filter type.
+template <int BPP>
+bool unfilter_bpp(const uint8_t* raw, int32_t height, size_t stride, uint8_t* out,
+                  const uint8_t* zero_row) {
   for (int32_t y = 0; y < height; ++y) {
     const uint8_t* in = raw + static_cast<size_t>(y) * (stride + 1);
-    const uint8_t ft = in[0];
-    ++in;
+    const uint8_t ft = *in++;
     uint8_t* row = out + static_cast<size_t>(y) * stride;
+    const uint8_t* prev = y ? row - stride : zero_row;
     switch (ft) {
       case 0:
         std::memcpy(row, in, stride);
         break;
-      case 1:
-        for (size_t i = 0; i < stride; ++i)
-          row[i] = static_cast<uint8_t>(in[i] + (i >= static_cast<size_t>(bpp) ? row[i - bpp] : 0));
+      case 1: {
+        uint8_t a[BPP] = {};
+        for (size_t i = 0; i < stride; i += BPP)
+          for (int k = 0; k < BPP; ++k) row[i + k] = a[k] = static_cast<uint8_t>(in[i + k] + a[k]);
         break;
+      }
       case 2:
-        for (size_t i = 0; i < stride; ++i) row[i] = static_cast<uint8_t>(in[i] + (prev ? prev[i] : 0));
+        for (size_t i = 0; i < stride; ++i) row[i] = static_cast<uint8_t>(in[i] + prev[i]);
         break;
-      case 3:
-        for (size_t i = 0; i < stride; ++i) {
-          const int a = i >= static_cast<size_t>(bpp) ? row[i - bpp] : 0;
-          const int b = prev ? prev[i] : 0;
-          row[i] = static_cast<uint8_t>(in[i] + ((a + b) >> 1));
-        }
+      case 3: {
+        int a[BPP] = {};
+        for (size_t i = 0; i < stride; i += BPP)
+          for (int k = 0; k < BPP; ++k) {
+            a[k] = static_cast<uint8_t>(in[i + k] + ((a[k] + prev[i + k]) >> 1));
+            row[i + k] = static_cast<uint8_t>(a[k]);
+          }
         break;
-      case 4:
-        for (size_t i = 0; i < stride; ++i) {
-          const int a = i >= static_cast<size_t>(bpp) ? row[i - bpp] : 0;
-          const int b = prev ? prev[i] : 0;
-          const int c = (prev && i >= static_cast<size_t>(bpp)) ? prev[i - bpp] : 0;
-          row[i] = static_cast<uint8_t>(in[i] + paeth(a, b, c));
-        }
+      }
+      case 4: {
+        int a[BPP] = {}, c[BPP] = {};
+        for (size_t i = 0; i < stride; i += BPP)
+          for (int k = 0; k < BPP; ++k) {
+            const int b = prev[i + k];
+            a[k] = static_cast<uint8_t>(in[i + k] + paeth(a[k], b, c[k]));
+            c[k] = b;
+            row[i + k] = static_cast<uint8_t>(a[k]);
+          }
         break;
+      }
       default:
         return false;
     }
-    prev = row;
   }
   return true;
+}
+
+bool unfilter(const uint8_t* raw, int32_t height, size_t stride, int bpp, uint8_t* out) {
+  std::vector<uint8_t> zero_row(stride, 0);
+  if (bpp == 1) return unfilter_bpp<1>(raw, height, stride, out, zero_row.data());
+  if (bpp == 3) return unfilter_bpp<3>(raw, height, stride, out, zero_row.data());
+  return unfilter_bpp<4>(raw, height, stride, out, zero_row.data());
 }
 
 // Walks the chunks of a PNG file: header into `h`, the IDAT payloads concatenated into
@@ -549,7 +599,7 @@ int decode_png(const char* path, const PngHeader& want, uint8_t* out, Scratch* s
   }
   const size_t stride = static_cast<size_t>(h.width) * h.channels;
   const size_t need = static_cast<size_t>(h.height) * (stride + 1);
-  s->raw.resize(need);
+  s->raw.resize(need + kCopySlack);
   if (!zlib_decode(s->idat.data(), s->idat.size(), s->raw.data(), need, why)) {
     *why = std::string(path) + ": " + *why;
     return CP_ERR_IO;

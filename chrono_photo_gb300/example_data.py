@@ -134,3 +134,49 @@ def job_specs(seed=4, count=512):
         w, h = res[int(rng.integers(0, 4))]
         jobs.append(dict(n=n, w=w, h=h, outlier=modes[int(rng.integers(0, 4))], seed=seed * 100000 + j))
     return jobs
+
+
+def _png_chunk(kind, body):
+    import struct
+    import zlib
+    return (struct.pack(">I", len(body)) + kind + body +
+            struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF))
+
+
+def encode_png(img, level=6):
+    """PNG bytes of a uint8 [h, w, c] image (c = 1, 3 or 4), every scanline Paeth-filtered
+    (filter type 4, the usual choice of encoders for photographs), zlib at `level`."""
+    import struct
+    import zlib
+    h, w, c = img.shape
+    x = img.reshape(h, w * c).astype(np.int16)
+    a = np.zeros_like(x)
+    a[:, c:] = x[:, :-c]
+    b = np.zeros_like(x)
+    b[1:] = x[:-1]
+    cc = np.zeros_like(x)
+    cc[1:, c:] = x[:-1, :-c]
+    p = a + b - cc
+    pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - cc)
+    pred = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, cc))
+    rows = np.empty((h, w * c + 1), np.uint8)
+    rows[:, 0] = 4
+    rows[:, 1:] = ((x - pred) & 0xFF).astype(np.uint8)
+    ihdr = struct.pack(">IIBBBBB", w, h, 8, {1: 0, 3: 2, 4: 6}[c], 0, 0, 0)
+    return (b"\x89PNG\r\n\x1a\n" + _png_chunk(b"IHDR", ihdr) +
+            _png_chunk(b"IDAT", zlib.compress(rows.tobytes(), level)) + _png_chunk(b"IEND", b""))
+
+
+def write_pngs(frames, directory, level=6, threads=8):
+    """Writes frames [n, h, w, c] as directory/frame_00000.png ... on a thread pool (zlib
+    releases the interpreter lock); returns the paths in frame order."""
+    import concurrent.futures as cf
+    import os
+
+    def one(i):
+        path = os.path.join(directory, "frame_%05d.png" % i)
+        with open(path, "wb") as f:
+            f.write(encode_png(frames[i], level))
+        return path
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(one, range(len(frames))))
