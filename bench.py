@@ -637,62 +637,14 @@ def run_serve(args):
         "clocks": clk.summary()}), flush=True)
 
 
-def _shake_frames_device(n, w, h, max_shift, seed):
-    """Seeded shake stack generated on the device (the host generator would take minutes at
-    this size): gradient + 8 random-phase sinusoids, translated per frame by U[-s, s]^2,
-    plus sigma-3 noise and 5 moving disks. Returns (uint8 [n, h, w, 3] tensor, shifts)."""
-    import numpy as np
-    import torch
-    rng = np.random.default_rng(seed)
-    shifts = rng.integers(-max_shift, max_shift + 1, size=(n, 2))
-    pad = max_shift + 1
-    bw, bh = w + 2 * pad, h + 2 * pad
-    dev = torch.device("cuda")
-    xs = torch.arange(bw, device=dev, dtype=torch.float32)[None, :]
-    ys = torch.arange(bh, device=dev, dtype=torch.float32)[:, None]
-    a = rng.uniform(40, 160, size=3)
-    b = rng.uniform(-40, 40, size=3)
-    d = rng.uniform(-40, 40, size=3)
-    tex = torch.zeros(bh, bw, device=dev)
-    for _ in range(8):
-        fx, fy = rng.uniform(0.04, 0.35, size=2)
-        tex += float(rng.uniform(6, 16)) * torch.sin(float(fx) * xs + float(fy) * ys + float(rng.uniform(0, 6.283)))
-    big = torch.stack([float(a[c]) + float(b[c]) * xs / bw + float(d[c]) * ys / bh + tex
-                       for c in range(3)], dim=-1)
-    out = torch.empty((n, h, w, 3), dtype=torch.uint8, device=dev)
-    gen = torch.Generator(device=dev)
-    gen.manual_seed(seed)
-    disks = [(rng.uniform(0, w), rng.uniform(0.4 * h, 0.6 * h), rng.uniform(0, w),
-              rng.uniform(0.4 * h, 0.6 * h), rng.uniform(20, 60), rng.integers(0, 256, size=3))
-             for _ in range(5)]
-    for i in range(n):
-        dx, dy = int(shifts[i][0]), int(shifts[i][1])
-        f = big[pad + dy:pad + dy + h, pad + dx:pad + dx + w] + \
-            3.0 * torch.randn((h, w, 3), generator=gen, device=dev)
-        t = i / max(n - 1, 1)
-        for (x0, y0, x1, y1, r, col) in disks:
-            cx, cy = x0 + (x1 - x0) * t, y0 + (y1 - y0) * t
-            xa, xb = max(int(cx - r) - 1, 0), min(int(cx + r) + 2, w)
-            ya, yb = max(int(cy - r) - 1, 0), min(int(cy + r) + 2, h)
-            if xa >= xb or ya >= yb:
-                continue
-            yy = torch.arange(ya, yb, device=dev, dtype=torch.float32)[:, None]
-            xx = torch.arange(xa, xb, device=dev, dtype=torch.float32)[None, :]
-            m = (xx - cx) ** 2 + (yy - cy) ** 2 <= r * r
-            f[ya:yb, xa:xb][m] = torch.tensor([float(v) for v in col], device=dev)
-        out[i] = torch.clamp(torch.floor(f + 0.5), 0, 255).to(torch.uint8)
-    torch.cuda.synchronize()
-    return out, shifts
-
-
 def run_shake(args):
     """Camera shake on 100 frames of 6000x4000: the offset search (4 anchors, radius 32,
     search radius 20) and the composite of the cropped stack (abs/0.05/0.2 extreme)."""
     import numpy as np
-    from chrono_photo_gb300 import make_params
+    from chrono_photo_gb300 import example_data, make_params
     ctx, lib, _abi, local = _ctx_and_lib()
     n, w, h, r, s = 100, 6000, 4000, 32, 20
-    frames, shifts = _shake_frames_device(n, w, h, 12, seed=5)
+    frames, shifts = example_data.shake_stack_device(n, w, h, 12, seed=5)
     fb = w * h * C
     base = frames.data_ptr()
     ptrs = (ct.c_void_p * n)(*[base + i * fb for i in range(n)])

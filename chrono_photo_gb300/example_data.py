@@ -180,3 +180,53 @@ def write_pngs(frames, directory, level=6, threads=8):
         return path
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
         return list(ex.map(one, range(len(frames))))
+
+
+def shake_stack_device(n, w, h, max_shift, seed):
+    """Seeded shake stack generated on the CUDA device with torch (the host generator would
+    take minutes at 100 x 6000x4000): gradient + 8 random-phase sinusoids, translated per frame
+    by U[-s, s]^2, plus sigma-3 noise and 5 moving disks. Returns (uint8 [n, h, w, 3] device
+    tensor, shifts); the shake offsets of frame i relative to frame 0 are shifts[0] - shifts[i]."""
+    import torch
+    rng = np.random.default_rng(seed)
+    shifts = rng.integers(-max_shift, max_shift + 1, size=(n, 2))
+    pad = max_shift + 1
+    bw, bh = w + 2 * pad, h + 2 * pad
+    dev = torch.device("cuda")
+    xs = torch.arange(bw, device=dev, dtype=torch.float32)[None, :]
+    ys = torch.arange(bh, device=dev, dtype=torch.float32)[:, None]
+    a = rng.uniform(40, 160, size=3)
+    b = rng.uniform(-40, 40, size=3)
+    d = rng.uniform(-40, 40, size=3)
+    tex = torch.zeros(bh, bw, device=dev)
+    for _ in range(8):
+        fx, fy = rng.uniform(0.04, 0.35, size=2)
+        tex += float(rng.uniform(6, 16)) * torch.sin(float(fx) * xs + float(fy) * ys + float(rng.uniform(0, 6.283)))
+    big = torch.stack([float(a[c]) + float(b[c]) * xs / bw + float(d[c]) * ys / bh + tex
+                       for c in range(3)], dim=-1)
+    # 16 spare bytes after the last frame: the kernels' 16-byte row copies may read past it
+    flat = torch.zeros(n * h * w * 3 + 16, dtype=torch.uint8, device=dev)
+    out = flat[:n * h * w * 3].view(n, h, w, 3)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    disks = [(rng.uniform(0, w), rng.uniform(0.4 * h, 0.6 * h), rng.uniform(0, w),
+              rng.uniform(0.4 * h, 0.6 * h), rng.uniform(20, 60), rng.integers(0, 256, size=3))
+             for _ in range(5)]
+    for i in range(n):
+        dx, dy = int(shifts[i][0]), int(shifts[i][1])
+        f = big[pad + dy:pad + dy + h, pad + dx:pad + dx + w] + \
+            3.0 * torch.randn((h, w, 3), generator=gen, device=dev)
+        t = i / max(n - 1, 1)
+        for (x0, y0, x1, y1, r, col) in disks:
+            cx, cy = x0 + (x1 - x0) * t, y0 + (y1 - y0) * t
+            xa, xb = max(int(cx - r) - 1, 0), min(int(cx + r) + 2, w)
+            ya, yb = max(int(cy - r) - 1, 0), min(int(cy + r) + 2, h)
+            if xa >= xb or ya >= yb:
+                continue
+            yy = torch.arange(ya, yb, device=dev, dtype=torch.float32)[:, None]
+            xx = torch.arange(xa, xb, device=dev, dtype=torch.float32)[None, :]
+            m = (xx - cx) ** 2 + (yy - cy) ** 2 <= r * r
+            f[ya:yb, xa:xb][m] = torch.tensor([float(v) for v in col], device=dev)
+        out[i] = torch.clamp(torch.floor(f + 0.5), 0, 255).to(torch.uint8)
+    torch.cuda.synchronize()
+    return out, shifts
