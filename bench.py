@@ -7,8 +7,11 @@ backward, --threshold rel/3/6 with --outlier average, and --mode darker / lighte
 Metric: megapixel-frames per second = 6 * 64 * 1920 * 1080 / 1e6 per step / time.
 
   value       device-resident frames, kernels only (CUDA events on the library's stream)
-  e2e         the same step through cp_composite with the frames in pinned host memory:
-              every step copies each composite's 64 frames host->device and the results back
+  e2e         the same step from pinned host memory through cp_composite_multi: every step
+              copies the 64 frames host->device once (band by band, overlapping the six
+              settings' kernels) and the six composites and four blend masks back
+  e2e_single_calls  the step as six cp_composite calls (the one-setting drop-in), each
+              copying the frames again
   roofline    the outlier kernel: algorithmic bytes (n*P*C read + 2*P*C written) per launch /
               its mean launch time, against the measured HBM copy bandwidth
   cpu_baseline  the C++ restatement of the reference (oracle/) on a band of rows, all cores
@@ -308,11 +311,27 @@ def run_gpu(args):
             if events is not None:
                 events[i][1].record(stream)
 
-    def e2e_step():
+    def e2e_single_calls():
         for p in params:
             rc = lib.cp_composite(h, ct.byref(hstack), ct.byref(p), out_host.value,
                                   blend_host.value if p.mode == 0 else None, None, None)
             ctx.check(rc, "cp_composite")
+
+    # one cp_composite_multi call per step: the stack crosses the host link once, the six
+    # composites and four blend masks come back into pinned memory
+    nv = len(params)
+    multi_ptr = ct.c_void_p()
+    ctx.check(lib.cp_host_alloc(h, 2 * nv * frame_bytes, ct.byref(multi_ptr)))
+    multi_params = (_abi.Params * nv)(*params)
+    multi_outs = (ct.c_void_p * nv)(*[multi_ptr.value + i * frame_bytes for i in range(nv)])
+    multi_blends = (ct.c_void_p * nv)(*[multi_ptr.value + (nv + i) * frame_bytes
+                                        if p.mode == 0 else None for i, p in enumerate(params)])
+    multi_warn = (ct.c_uint64 * nv)()
+
+    def e2e_step():
+        rc = lib.cp_composite_multi(h, ct.byref(hstack), multi_params, nv, multi_outs,
+                                    multi_blends, multi_warn)
+        ctx.check(rc, "cp_composite_multi")
 
     # ---- device-resident timing -------------------------------------------------------------
     for _ in range(args.warmup):
@@ -346,6 +365,15 @@ def run_gpu(args):
         e2e_step()
     e2e_s = barrier_max(time.perf_counter() - t0)
     e2e_value = ws * args.steps * len(VARIANTS) * MPXF_PER_COMPOSITE / e2e_s
+    # the drop-in form: one cp_composite per setting, each uploading the stack again
+    single_steps = max(1, min(args.steps, 20))
+    e2e_single_calls()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(single_steps):
+        e2e_single_calls()
+    single_s = barrier_max(time.perf_counter() - t0)
+    single_value = ws * single_steps * len(VARIANTS) * MPXF_PER_COMPOSITE / single_s
 
     if rank != 0:
         return
@@ -374,8 +402,15 @@ def run_gpu(args):
         "data": "synthetic (seeded disk-over-gradient stacks)", "config": CONFIG,
         "variants_ms": {name: round(t, 4) for (name, _), t in zip(VARIANTS, per_var)},
         "e2e": {"value": e2e_value, "unit": METRIC,
-                "h2d_bytes_per_step": len(VARIANTS) * N_FRAMES * frame_bytes,
-                "d2h_bytes_per_step": (len(VARIANTS) + 4) * frame_bytes},
+                "h2d_bytes_per_step": N_FRAMES * frame_bytes,
+                "d2h_bytes_per_step": (len(VARIANTS) + 4) * frame_bytes,
+                "call": "cp_composite_multi: the stack from pinned host memory once per step, "
+                        "six composites + four blend masks back"},
+        "e2e_single_calls": {"value": single_value, "unit": METRIC, "steps": single_steps,
+                             "h2d_bytes_per_step": len(VARIANTS) * N_FRAMES * frame_bytes,
+                             "d2h_bytes_per_step": (len(VARIANTS) + 4) * frame_bytes,
+                             "call": "six cp_composite calls (the drop-in for one "
+                                     "OutlierProcessor / SimpleProcessor run each)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "kernel": "k_composite<3> (outlier)", "peak_kind": peak_kind},

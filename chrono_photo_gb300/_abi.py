@@ -65,6 +65,8 @@ class JobResult(ct.Structure):
                 ("admit_s", ct.c_double), ("done_s", ct.c_double)]
 
 
+CP_MAX_SETTINGS = 16
+
 P = ct.c_void_p
 I32 = ct.c_int32
 I32P = ct.POINTER(ct.c_int32)
@@ -97,6 +99,8 @@ SIGNATURES = [
                                        ct.POINTER(Debug), P, P]),
     ("cp_composite", ct.c_int, [P, ct.POINTER(Stack), ct.POINTER(Params), P, P,
                                 ct.POINTER(Debug), U64P]),
+    ("cp_composite_multi", ct.c_int, [P, ct.POINTER(Stack), ct.POINTER(Params), I32,
+                                      ct.POINTER(P), ct.POINTER(P), U64P]),
     ("cp_composite_batch_device", ct.c_int, [P, ct.POINTER(Stack), ct.POINTER(Params), I32,
                                              ct.POINTER(P), ct.POINTER(P), P, P]),
     ("cp_composite_video_device", ct.c_int, [P, ct.POINTER(P), I32, I32, I32, I32, I32, I64P,

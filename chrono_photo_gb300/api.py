@@ -248,6 +248,26 @@ class Context:
             return out, bl, warn.value, dbg_arrays
         return out, bl, warn.value
 
+    def composite_multi(self, frames, params_list, blend=True):
+        """One host-memory stack under several parameter sets (cp_composite_multi): the
+        frames are copied to the device once. Returns [(composite, blend_mask or None,
+        warnings)] in the order of params_list."""
+        a = _as_stack(frames)
+        n, h, w, c = a.shape
+        k = len(params_list)
+        st = _abi.Stack(n=n, width=w, height=h, channels=c, base=a.ctypes.data,
+                        frame_stride=h * w * c)
+        ps = (_abi.Params * k)(*params_list)
+        outs = [np.empty((h, w, c), dtype=np.uint8) for _ in range(k)]
+        bls = [np.empty((h, w, c), dtype=np.uint8) if blend and p.mode == 0 else None
+               for p in params_list]
+        optr = (ct.c_void_p * k)(*[o.ctypes.data for o in outs])
+        bptr = (ct.c_void_p * k)(*[b.ctypes.data if b is not None else None for b in bls])
+        warn = (ct.c_uint64 * k)()
+        self.check(lib().cp_composite_multi(self.handle, ct.byref(st), ps, k, optr, bptr, warn),
+                   "cp_composite_multi")
+        return [(outs[i], bls[i], int(warn[i])) for i in range(k)]
+
     def shake_analyze(self, frames, anchors, anchor_radius, search_radius, diffs=False):
         """ShakeAnalyzer::analyze on the device: per-frame (dx, dy) offsets."""
         a = _as_stack(frames)

@@ -5,7 +5,8 @@
 // copies: 95-135 GB/s on GB300 for 2-32 MB copies, 207 GB/s with two streams); the kernel of
 // band b runs while band b+1 is in flight, and each band's result is copied back on a
 // fourth stream as soon as its kernel is done. Equally strided frames move as one 2D copy
-// per band and stream.
+// per band and stream. cp_composite_multi runs several parameter sets over each band, so the
+// frames cross the host link once for all of them.
 
 #include <cuda_runtime.h>
 
@@ -37,10 +38,19 @@ int ensure_events(cp_ctx* ctx, size_t count) {
 
 }  // namespace
 
-extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
-                            uint8_t* out, uint8_t* out_blend, const cp_debug* dbg,
-                            uint64_t* n_warnings) {
-  if (!ctx || !stack || !params || !out) return CP_ERR_ARG;
+// The warning counters of the settings follow the error flags in the context's 256-byte
+// flag block (cp_ctx_create).
+static_assert(64 + 8 * CP_MAX_SETTINGS <= 256, "warning counters exceed the flag block");
+
+// The host-staged composite of one stack under `count` parameter sets (cp_composite is
+// count = 1, the only form that takes diagnostics).
+static int composite_staged(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                            int count, uint8_t* const* outs, uint8_t* const* blends,
+                            const cp_debug* dbg, uint64_t* n_warnings) {
+  if (!ctx || !stack || !params || !outs || count < 1) return CP_ERR_ARG;
+  if (count > CP_MAX_SETTINGS) return CP_ERR_LIMIT;
+  for (int k = 0; k < count; ++k)
+    if (!outs[k]) return CP_ERR_ARG;
   if (stack->n < 1 || stack->n > CP_MAX_FRAMES || (!stack->frames && !stack->base))
     return CP_ERR_ARG;
   std::lock_guard<std::mutex> call(ctx->call_mu);
@@ -54,22 +64,34 @@ extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params*
   const uint64_t pitch = round_up(frame_bytes + 16, kFrameAlign);
   const uint64_t P = static_cast<uint64_t>(stack->width) * stack->height;
   const uint64_t out_bytes = P * C;
+  const uint64_t ostride = round_up(out_bytes, 256);  // one setting's output in out_dev
+  std::vector<bool> want_blend(static_cast<size_t>(count));
+  bool any_blend = false;
+  for (int k = 0; k < count; ++k) {
+    want_blend[static_cast<size_t>(k)] =
+        blends && blends[k] && params[k].mode == CP_MODE_OUTLIER;
+    any_blend = any_blend || want_blend[static_cast<size_t>(k)];
+  }
   int rc = ensure_buffer(ctx, ctx->frames_dev, pitch * n);
-  if (!rc) rc = ensure_buffer(ctx, ctx->out_dev, round_up(out_bytes, 256));
-  const bool want_blend = out_blend && params->mode == CP_MODE_OUTLIER;
-  if (!rc && want_blend) rc = ensure_buffer(ctx, ctx->blend_dev, round_up(out_bytes, 256));
+  if (!rc) rc = ensure_buffer(ctx, ctx->out_dev, ostride * count);
+  if (!rc && any_blend) rc = ensure_buffer(ctx, ctx->blend_dev, ostride * count);
   if (rc) return rc;
 
-  // device frame table
+  // device frame table and one descriptor per setting
   uint8_t* fdev = static_cast<uint8_t*>(ctx->frames_dev.ptr);
   std::vector<const uint8_t*> dev_frames(static_cast<size_t>(n));
   for (int i = 0; i < n; ++i) dev_frames[static_cast<size_t>(i)] = fdev + pitch * i;
-  StackDev d;
-  rc = prepare_stack(ctx, stack, params, dev_frames.data(), &d);
-  if (rc) return rc;
-  d.out = static_cast<uint8_t*>(ctx->out_dev.ptr);
-  d.blend = want_blend ? static_cast<uint8_t*>(ctx->blend_dev.ptr) : nullptr;
-  d.warnings = ctx->d_warn;
+  std::vector<StackDev> ds(static_cast<size_t>(count));
+  for (int k = 0; k < count; ++k) {
+    StackDev& d = ds[static_cast<size_t>(k)];
+    rc = prepare_stack(ctx, stack, &params[k], dev_frames.data(), &d);
+    if (rc) return rc;
+    d.out = static_cast<uint8_t*>(ctx->out_dev.ptr) + ostride * k;
+    d.blend = want_blend[static_cast<size_t>(k)]
+                  ? static_cast<uint8_t*>(ctx->blend_dev.ptr) + ostride * k
+                  : nullptr;
+    d.warnings = ctx->d_warn + k;  // CP_MAX_SETTINGS counters behind the error flags
+  }
 
   // optional diagnostics: device arrays, copied back at the end
   const int words = (n + 31) / 32;
@@ -79,7 +101,8 @@ extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params*
     uint64_t off;
   };
   std::vector<DbgPart> parts;
-  if (dbg && params->mode == CP_MODE_OUTLIER) {
+  StackDev& d = ds[0];
+  if (dbg && count == 1 && params->mode == CP_MODE_OUTLIER) {
     uint64_t off = 0;
     auto add = [&](void* h, uint64_t bytes) {
       if (!h) return;
@@ -109,14 +132,16 @@ extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params*
     }
   }
 
-  rc = cuda_status(ctx, cudaMemsetAsync(ctx->d_warn, 0, sizeof(unsigned long long), ctx->stream),
-                   "memset");
+  rc = cuda_status(ctx, cudaMemsetAsync(ctx->d_warn, 0, sizeof(unsigned long long) * count,
+                                        ctx->stream), "memset");
   if (rc) return rc;
 
   // bands: flat pixel ranges in whole tiles; cropped stacks move whole frames at once
   int bands = 1;
   if (!crop && P >= static_cast<uint64_t>(kTilePx) * ctx->sm_count * 4) bands = 4;
-  rc = ensure_events(ctx, static_cast<size_t>(3 * bands));
+  // per band: two copies landed, then one kernel done per setting
+  const int ev_band = 2 + count;
+  rc = ensure_events(ctx, static_cast<size_t>(ev_band * bands));
   if (rc) return rc;
   const uint64_t tiles_total = (P + kTilePx - 1) / kTilePx;
   auto host_frame = [&](int i) -> const uint8_t* {
@@ -157,37 +182,39 @@ extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params*
         if (rc) return rc;
       }
     }
-    cudaEvent_t copied = ctx->band_events[static_cast<size_t>(3 * b)];
-    cudaEvent_t copied2 = ctx->band_events[static_cast<size_t>(3 * b + 2)];
-    cudaEvent_t done = ctx->band_events[static_cast<size_t>(3 * b + 1)];
+    cudaEvent_t copied = ctx->band_events[static_cast<size_t>(ev_band * b)];
+    cudaEvent_t copied2 = ctx->band_events[static_cast<size_t>(ev_band * b + 1)];
     cudaEventRecord(copied, cs[0]);
     cudaEventRecord(copied2, cs[1]);
     cudaStreamWaitEvent(ctx->stream, copied, 0);
     cudaStreamWaitEvent(ctx->stream, copied2, 0);
-    StackDev db = d;
-    if (!crop) {
-      db.px_begin = static_cast<int32_t>(px0);
-      db.px_end = static_cast<int32_t>(px1);
-      db.tiles = static_cast<int32_t>(t1 - t0);
-    }
-    rc = launch_single(ctx, db, ctx->stream);
-    if (rc) return rc;
-    cudaEventRecord(done, ctx->stream);
-    cudaStreamWaitEvent(ctx->d2h_stream, done, 0);
     const uint64_t o0 = crop ? 0 : px0 * C, ob = crop ? out_bytes : (px1 - px0) * C;
-    rc = cuda_status(ctx, cudaMemcpyAsync(out + o0, d.out + o0, ob, cudaMemcpyDeviceToHost,
-                                          ctx->d2h_stream), "d2h");
-    if (!rc && want_blend)
-      rc = cuda_status(ctx, cudaMemcpyAsync(out_blend + o0, d.blend + o0, ob,
+    for (int k = 0; k < count; ++k) {
+      StackDev db = ds[static_cast<size_t>(k)];
+      if (!crop) {
+        db.px_begin = static_cast<int32_t>(px0);
+        db.px_end = static_cast<int32_t>(px1);
+        db.tiles = static_cast<int32_t>(t1 - t0);
+      }
+      rc = launch_single(ctx, db, ctx->stream);
+      if (rc) return rc;
+      cudaEvent_t done = ctx->band_events[static_cast<size_t>(ev_band * b + 2 + k)];
+      cudaEventRecord(done, ctx->stream);
+      cudaStreamWaitEvent(ctx->d2h_stream, done, 0);
+      rc = cuda_status(ctx, cudaMemcpyAsync(outs[k] + o0, db.out + o0, ob,
                                             cudaMemcpyDeviceToHost, ctx->d2h_stream), "d2h");
-    if (rc) return rc;
+      if (!rc && db.blend)
+        rc = cuda_status(ctx, cudaMemcpyAsync(blends[k] + o0, db.blend + o0, ob,
+                                              cudaMemcpyDeviceToHost, ctx->d2h_stream), "d2h");
+      if (rc) return rc;
+    }
   }
-  uint64_t warn = 0;
+  uint64_t warn[CP_MAX_SETTINGS] = {};
   cudaEvent_t all = ctx->band_events[0];
   cudaEventRecord(all, ctx->stream);
   cudaStreamWaitEvent(ctx->d2h_stream, all, 0);
-  rc = cuda_status(ctx, cudaMemcpyAsync(&warn, ctx->d_warn, sizeof warn, cudaMemcpyDeviceToHost,
-                                        ctx->d2h_stream), "d2h");
+  rc = cuda_status(ctx, cudaMemcpyAsync(warn, ctx->d_warn, sizeof(uint64_t) * count,
+                                        cudaMemcpyDeviceToHost, ctx->d2h_stream), "d2h");
   if (rc) return rc;
   for (const auto& part : parts) {
     rc = cuda_status(ctx, cudaMemcpyAsync(part.host, static_cast<uint8_t*>(ctx->dbg_dev.ptr) + part.off,
@@ -199,6 +226,19 @@ extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params*
   if (rc) return rc;
   rc = check_device_error(ctx);
   if (rc) return rc;
-  if (n_warnings) *n_warnings = warn;
+  if (n_warnings)
+    for (int k = 0; k < count; ++k) n_warnings[k] = warn[k];
   return CP_OK;
+}
+
+extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                            uint8_t* out, uint8_t* out_blend, const cp_debug* dbg,
+                            uint64_t* n_warnings) {
+  return composite_staged(ctx, stack, params, 1, &out, &out_blend, dbg, n_warnings);
+}
+
+extern "C" int cp_composite_multi(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                                  int32_t count, uint8_t* const* out, uint8_t* const* out_blend,
+                                  uint64_t* n_warnings) {
+  return composite_staged(ctx, stack, params, count, out, out_blend, nullptr, n_warnings);
 }

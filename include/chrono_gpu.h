@@ -43,7 +43,7 @@ extern "C" {
 #define CP_ERR_RANGE (-6)   /* shake window outside the image (reference: panic, shake.rs:336) */
 #define CP_ERR_STATE (-7)   /* object in the wrong state (stopped server, unknown job)     */
 #define CP_ERR_NODEV (-8)   /* no CUDA device with compute capability 10.3                 */
-#define CP_ERR_LIMIT (-9)   /* request above a fixed limit of cp_composite_batch_static    */
+#define CP_ERR_LIMIT (-9)   /* request above a fixed limit (batch_static, composite_multi) */
 #define CP_ERR_IO (-10)     /* image file missing, unreadable or not a supported PNG       */
 
 /* ---- option enums (src/options.rs) --------------------------------------------------- */
@@ -199,6 +199,18 @@ int cp_composite_device(cp_ctx* ctx, const cp_stack* stack, const cp_params* par
  * dbg members, when given, are host arrays. */
 int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params* params, uint8_t* out,
                  uint8_t* out_blend, const cp_debug* dbg, uint64_t* n_warnings);
+
+/* cp_composite of one host-memory stack under `count` parameter sets (1..CP_MAX_SETTINGS):
+ * the frames cross the host link once, band by band, and every setting's kernel runs on
+ * each band while the next band is in flight. out[k], out_blend[k] (array and entries
+ * nullable) and n_warnings[k] (nullable) belong to params[k]; each equals what cp_composite
+ * gives for params[k] alone. The reference composites one setting per run, re-reading its
+ * frames each time (src/main.rs:454-517); this is the call for several settings of one
+ * stack (e.g. comparing thresholds or outlier modes). CP_ERR_LIMIT above CP_MAX_SETTINGS. */
+#define CP_MAX_SETTINGS 16
+int cp_composite_multi(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                       int32_t count, uint8_t* const* out, uint8_t* const* out_blend,
+                       uint64_t* n_warnings);
 
 /* Many stacks of uneven size in ONE persistent launch that pulls (stack, tile) work items
  * from a device queue (chrono-video windows, mixed jobs). Device pointers; params[i]

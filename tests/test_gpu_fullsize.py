@@ -99,6 +99,17 @@ def test_hd_device_entry_point_equals_host(ctx, hd):
             ctx.free(q)
 
 
+def test_hd_multi_settings_equal_single_calls(ctx, hd):
+    """The benchmark's six settings in one cp_composite_multi call (the stack uploaded once)
+    equal six cp_composite calls, every pixel, warnings included."""
+    ps = [cases.params(**kw) for kw in HD_SETTINGS[:6]]
+    for p, (o, b, wn) in zip(ps, ctx.composite_multi(hd, ps)):
+        ref = ctx.composite(hd, p)
+        assert np.array_equal(o, ref[0])
+        assert (b is None and ref[1] is None) or np.array_equal(b, ref[1])
+        assert wn == ref[2]
+
+
 VIDEO_ROWS = [0, 1, 134, 270, 405, 539, 540, 675, 810, 945, 1078, 1079]
 
 

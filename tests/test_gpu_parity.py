@@ -204,6 +204,43 @@ def test_device_entry_point_matches_host(ctx, small):
             ctx.free(q)
 
 
+MULTI_SETTINGS = [
+    dict(mode="outlier", threshold="abs/0.05/0.2", outlier="average", background="first"),
+    dict(mode="outlier", threshold="rel/3/6", outlier="extreme", background="random"),
+    dict(mode="darker"),
+    dict(mode="outlier", threshold="abs/0.1/0.3", outlier="forward", background="average",
+         fade="clamp/rel/0,0.2/8,1"),
+    dict(mode="lighter", weights=[0.3, 0.6, 0.1, 1]),
+    dict(mode="outlier", threshold="abs/0.02", outlier="backward", background="median",
+         sample=[0, 2, 4, 6, 8, 10, 12, 14]),
+]
+
+
+def test_composite_multi_matches_single_calls(ctx, small):
+    """cp_composite_multi (one upload, several settings) gives each setting exactly what
+    cp_composite gives it alone, warnings included."""
+    ps = [cases.params(**kw) for kw in MULTI_SETTINGS]
+    got = ctx.composite_multi(small, ps)
+    for p, (o, b, wn) in zip(ps, got):
+        ref = ctx.composite(small, p)
+        assert np.array_equal(o, ref[0])
+        assert (b is None and ref[1] is None) or np.array_equal(b, ref[1])
+        assert wn == ref[2]
+        oref = oracle.composite(small, p, threads=8)
+        cases.assert_close_u8(o, oref[0], what="composite")
+
+
+def test_composite_multi_limits(ctx, small):
+    p = cases.params()
+    with pytest.raises(_abi.ChronoError) as e:
+        ctx.composite_multi(small, [p] * (_abi.CP_MAX_SETTINGS + 1))
+    assert e.value.status == _abi.CP_ERR_LIMIT
+    with pytest.raises(_abi.ChronoError) as e:
+        ctx.composite_multi(small, [])
+    assert e.value.status == _abi.CP_ERR_ARG
+    assert len(ctx.composite_multi(small, [p] * _abi.CP_MAX_SETTINGS)) == _abi.CP_MAX_SETTINGS
+
+
 def test_invalid_stacks(ctx):
     f = np.zeros((129, 2, 2, 3), np.uint8)
     with pytest.raises(_abi.ChronoError) as e:
