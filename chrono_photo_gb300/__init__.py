@@ -7,4 +7,4 @@ the reference's processor interface in Python (api.py).
 from ._abi import ChronoError, lib  # noqa: F401
 from .api import (Context, Crop, Fade, OutlierProcessor, Server, ShakeAnalyzer,  # noqa: F401
                   SimpleProcessor, Threshold, default_context, load_png, make_params,
-                  png_info, video_windows)
+                  png_info, save_png, video_windows)

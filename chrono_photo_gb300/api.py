@@ -394,6 +394,18 @@ def load_png(paths, threads=0, out=None, context=None):
     return out
 
 
+def save_png(path, image, level=6, context=None):
+    """Writes a uint8 [h, w, c] image (c = 1, 3 or 4) as a PNG file (cp_save_png), creating a
+    missing parent directory like the reference's save_image (src/main.rs:519-570)."""
+    a = np.ascontiguousarray(image, dtype=np.uint8)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    h, w, c = a.shape
+    handle = context.handle if context else None
+    _check(handle, lib().cp_save_png(handle, str(path).encode(), a.ctypes.data, w, h, c,
+                                     int(level)), "cp_save_png")
+
+
 def video_windows(image_count, video_in, video_out=(None, None, 1)):
     """chrono-video windows of src/main.rs:230-286: list of (output frame, indices)."""
     (a, b, s), (c, d, t) = video_in, video_out

@@ -22,17 +22,17 @@
 
 #include "../../include/chrono_gpu.h"
 #include "cp_host_internal.h"
+#include "cp_png.h"
 
 namespace {
+
+using cp::png::adler32;
+using cp::png::be32;
+using cp::png::crc32_png;
 
 struct PngHeader {
   int32_t width = 0, height = 0, channels = 0;
 };
-
-uint32_t be32(const uint8_t* p) {
-  return (static_cast<uint32_t>(p[0]) << 24) | (static_cast<uint32_t>(p[1]) << 16) |
-         (static_cast<uint32_t>(p[2]) << 8) | static_cast<uint32_t>(p[3]);
-}
 
 bool read_file(const char* path, std::vector<uint8_t>* data) {
   FILE* f = std::fopen(path, "rb");
@@ -44,54 +44,6 @@ bool read_file(const char* path, std::vector<uint8_t>* data) {
   const bool ok = !std::ferror(f);
   std::fclose(f);
   return ok;
-}
-
-// ---- CRC-32 of the PNG chunks (ISO 3309 polynomial, reflected 0xEDB88320), slice-by-8 ----
-
-struct CrcTables {
-  uint32_t t[8][256];
-  CrcTables() {
-    for (uint32_t i = 0; i < 256; ++i) {
-      uint32_t c = i;
-      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-      t[0][i] = c;
-    }
-    for (int s = 1; s < 8; ++s)
-      for (uint32_t i = 0; i < 256; ++i) t[s][i] = (t[s - 1][i] >> 8) ^ t[0][t[s - 1][i] & 0xFF];
-  }
-};
-
-uint32_t crc32_png(const uint8_t* p, size_t n) {
-  static const CrcTables T;
-  uint32_t c = 0xFFFFFFFFu;
-  while (n >= 8) {
-    const uint32_t lo = c ^ (p[0] | (p[1] << 8) | (p[2] << 16) | (static_cast<uint32_t>(p[3]) << 24));
-    const uint32_t hi = p[4] | (p[5] << 8) | (p[6] << 16) | (static_cast<uint32_t>(p[7]) << 24);
-    c = T.t[7][lo & 0xFF] ^ T.t[6][(lo >> 8) & 0xFF] ^ T.t[5][(lo >> 16) & 0xFF] ^ T.t[4][lo >> 24] ^
-        T.t[3][hi & 0xFF] ^ T.t[2][(hi >> 8) & 0xFF] ^ T.t[1][(hi >> 16) & 0xFF] ^ T.t[0][hi >> 24];
-    p += 8;
-    n -= 8;
-  }
-  while (n--) c = T.t[0][(c ^ *p++) & 0xFF] ^ (c >> 8);
-  return c ^ 0xFFFFFFFFu;
-}
-
-// ---- Adler-32 of the zlib stream's decompressed data (RFC 1950 section 9) ----
-
-uint32_t adler32(const uint8_t* p, size_t n) {
-  uint32_t a = 1, b = 0;
-  while (n > 0) {
-    // 5552 is the largest run for which b cannot overflow 32 bits before the reduction.
-    size_t run = n < 5552 ? n : 5552;
-    n -= run;
-    while (run--) {
-      a += *p++;
-      b += a;
-    }
-    a %= 65521u;
-    b %= 65521u;
-  }
-  return (b << 16) | a;
 }
 
 // ---- DEFLATE decoder (RFC 1951) writing into a buffer of known size ----

@@ -1,0 +1,74 @@
+// cp_png.h — checksums of the PNG container shared by the frame reader (cp_ingest.cpp) and
+// the image writer (cp_png_write.cpp): the CRC-32 of every PNG chunk (ISO/IEC 15948, ISO 3309
+// polynomial) and the Adler-32 of the zlib stream (RFC 1950 section 9), plus the big-endian
+// integer helpers of both formats.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+namespace cp {
+namespace png {
+
+inline uint32_t be32(const uint8_t* p) {
+  return (static_cast<uint32_t>(p[0]) << 24) | (static_cast<uint32_t>(p[1]) << 16) |
+         (static_cast<uint32_t>(p[2]) << 8) | static_cast<uint32_t>(p[3]);
+}
+inline void put_be32(uint8_t* p, uint32_t v) {
+  p[0] = static_cast<uint8_t>(v >> 24);
+  p[1] = static_cast<uint8_t>(v >> 16);
+  p[2] = static_cast<uint8_t>(v >> 8);
+  p[3] = static_cast<uint8_t>(v);
+}
+
+// CRC-32 (reflected polynomial 0xEDB88320), slice-by-8; crc32_update continues a running
+// CRC (start from 0).
+struct CrcTables {
+  uint32_t t[8][256];
+  CrcTables() {
+    for (uint32_t i = 0; i < 256; ++i) {
+      uint32_t c = i;
+      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      t[0][i] = c;
+    }
+    for (int s = 1; s < 8; ++s)
+      for (uint32_t i = 0; i < 256; ++i) t[s][i] = (t[s - 1][i] >> 8) ^ t[0][t[s - 1][i] & 0xFF];
+  }
+};
+
+inline uint32_t crc32_update(uint32_t crc, const uint8_t* p, size_t n) {
+  static const CrcTables T;
+  uint32_t c = crc ^ 0xFFFFFFFFu;
+  while (n >= 8) {
+    const uint32_t lo = c ^ (p[0] | (p[1] << 8) | (p[2] << 16) | (static_cast<uint32_t>(p[3]) << 24));
+    const uint32_t hi = p[4] | (p[5] << 8) | (p[6] << 16) | (static_cast<uint32_t>(p[7]) << 24);
+    c = T.t[7][lo & 0xFF] ^ T.t[6][(lo >> 8) & 0xFF] ^ T.t[5][(lo >> 16) & 0xFF] ^ T.t[4][lo >> 24] ^
+        T.t[3][hi & 0xFF] ^ T.t[2][(hi >> 8) & 0xFF] ^ T.t[1][(hi >> 16) & 0xFF] ^ T.t[0][hi >> 24];
+    p += 8;
+    n -= 8;
+  }
+  while (n--) c = T.t[0][(c ^ *p++) & 0xFF] ^ (c >> 8);
+  return c ^ 0xFFFFFFFFu;
+}
+
+// Adler-32 (RFC 1950 section 9).
+inline uint32_t adler32(const uint8_t* p, size_t n) {
+  uint32_t a = 1, b = 0;
+  while (n > 0) {
+    // 5552 is the largest run for which b cannot overflow 32 bits before the reduction.
+    size_t run = n < 5552 ? n : 5552;
+    n -= run;
+    while (run--) {
+      a += *p++;
+      b += a;
+    }
+    a %= 65521u;
+    b %= 65521u;
+  }
+  return (b << 16) | a;
+}
+
+inline uint32_t crc32_png(const uint8_t* p, size_t n) { return crc32_update(0, p, n); }
+
+}  // namespace png
+}  // namespace cp
