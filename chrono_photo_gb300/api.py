@@ -9,10 +9,12 @@
     Crop::create (shake.rs:136-176)              Crop.create(offsets, width, height)
 
 Frames are numpy uint8 arrays [n, height, width, channels] (or a list of [h, w, c] arrays):
-the decoded images the reference reads through `image::open`. Every call runs on the GPU;
-there is no CPU path.
+the decoded images the reference reads through `image::open`; the processors also take a
+list of PNG file paths, as the reference's take files (decoded by cp_load_png). Every
+composite runs on the GPU; there is no CPU path.
 """
 import ctypes as ct
+import os
 
 import numpy as np
 
@@ -133,13 +135,34 @@ def make_params(mode="outlier", threshold=None, outlier="extreme", background="r
     return p
 
 
+def _is_paths(frames):
+    return isinstance(frames, (list, tuple)) and len(frames) > 0 and \
+        all(isinstance(f, (str, os.PathLike)) for f in frames)
+
+
 def _as_stack(frames):
+    """uint8 [n, h, w, c] from an array, a sequence of images, or a sequence of PNG file
+    paths (decoded by cp_load_png on all host threads, as the reference's processors take
+    their frames as files)."""
+    if _is_paths(frames):
+        return load_png(frames)
     if isinstance(frames, np.ndarray):
         a = np.ascontiguousarray(frames, dtype=np.uint8)
         if a.ndim == 3:
             a = a[..., None]
         return a
     return np.ascontiguousarray(np.stack([np.asarray(f, dtype=np.uint8) for f in frames]))
+
+
+def _select(frames, image_indices):
+    """The stack of the frames at image_indices (all when None) and its frame offset
+    (src/chrono.rs:103): paths are selected before decoding."""
+    if image_indices is None:
+        return _as_stack(frames), 0
+    idx = [int(i) for i in image_indices]
+    if _is_paths(frames):
+        return _as_stack([frames[i] for i in idx]), idx[0]
+    return np.ascontiguousarray(_as_stack(frames)[idx]), idx[0]
 
 
 class Context:
@@ -313,13 +336,10 @@ class OutlierProcessor:
         self.ctx = context
 
     def process(self, frames, image_indices=None, debug=False):
-        """(composite, blend mask) like OutlierProcessor::process (src/chrono.rs:73-206)."""
+        """(composite, blend mask) like OutlierProcessor::process (src/chrono.rs:73-206).
+        frames: uint8 [n, h, w, c], a sequence of images, or PNG file paths."""
         ctx = self.ctx or default_context()
-        a = _as_stack(frames)
-        offset = 0
-        if image_indices is not None:
-            a = np.ascontiguousarray(a[list(image_indices)])
-            offset = int(image_indices[0])
+        a, offset = _select(frames, image_indices)
         r = ctx.composite(a, frame_offset=offset, debug=debug, **self.kw)
         return r if debug else (r[0], r[1])
 
@@ -333,11 +353,7 @@ class SimpleProcessor:
 
     def process(self, frames, crop=None, image_indices=None):
         ctx = self.ctx or default_context()
-        a = _as_stack(frames)
-        offset = 0
-        if image_indices is not None:
-            a = np.ascontiguousarray(a[list(image_indices)])
-            offset = int(image_indices[0])
+        a, offset = _select(frames, image_indices)
         return ctx.composite(a, frame_offset=offset, blend=False, crop=crop, **self.kw)[0]
 
 

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from chrono_photo_gb300 import _abi, example_data
+from chrono_photo_gb300 import api as cg_api
 from oracle import oracle
 from tests import cases
 
@@ -250,3 +251,17 @@ def test_invalid_stacks(ctx):
         ctx.composite(np.zeros((2, 2, 2, 3), np.uint8), cases.params(threshold="rel/1/2"))
     with pytest.raises(_abi.ChronoError):
         ctx.composite(np.zeros((4, 2, 2, 2), np.uint8), cases.params())
+
+
+def test_processors_take_png_paths(ctx, small, tmp_path):
+    """OutlierProcessor / SimpleProcessor on PNG file paths (decoded by cp_load_png, only the
+    selected frames) equal the same calls on the arrays."""
+    paths = example_data.write_pngs(small, str(tmp_path), level=1, threads=4)
+    sel = list(range(3, 15))
+    op = cg_api.OutlierProcessor(threshold="abs/0.05/0.2", background="first",
+                                 outlier="forward", fade="clamp/abs/0,0.3/10,1", context=ctx)
+    a = op.process(small, image_indices=sel)
+    b = op.process(paths, image_indices=sel)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    sp = cg_api.SimpleProcessor(darker=False, context=ctx)
+    assert np.array_equal(sp.process(small), sp.process(paths))
