@@ -220,7 +220,7 @@ class Matcher {
       if (pos + kMinMatch <= n_) {
         const uint32_t h = hash(pos);
         const int max_len = static_cast<int>(std::min<size_t>(kMaxMatch, n_ - pos));
-        int cand = head_[h];
+        int64_t cand = head_[h];
         for (int chain = e_.chain; cand >= 0 && chain > 0; --chain) {
           const size_t dist = pos - static_cast<size_t>(cand);
           if (dist > static_cast<size_t>(kWindow)) break;
@@ -234,7 +234,7 @@ class Matcher {
               if (l >= e_.nice || l >= max_len) break;
             }
           }
-          const int nxt = prev_[static_cast<size_t>(cand) & (kWindow - 1)];
+          const int64_t nxt = prev_[static_cast<size_t>(cand) & (kWindow - 1)];
           if (nxt >= cand) break;
           cand = nxt;
         }
@@ -262,12 +262,12 @@ class Matcher {
   }
   void insert(size_t p, uint32_t h) {
     prev_[p & (kWindow - 1)] = head_[h];
-    head_[h] = static_cast<int>(p);
+    head_[h] = static_cast<int64_t>(p);
   }
   const uint8_t* d_;
   size_t n_;
   Effort e_;
-  std::vector<int> head_, prev_;
+  std::vector<int64_t> head_, prev_;  // positions; -1: none
 };
 
 // Fixed Huffman code lengths (RFC 1951 section 3.2.6).
