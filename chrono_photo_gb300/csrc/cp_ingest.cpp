@@ -60,9 +60,10 @@ struct Huffman {
   uint16_t fast[1 << kFast];
 };
 
-// Builds `h` from per-symbol code lengths. False when the lengths over-subscribe the code
-// space; incomplete codes are accepted (an unassigned code then fails at decode time).
-bool build_huffman(Huffman* h, const uint8_t* lengths, int n) {
+// The counts per code length and the symbols in canonical order from per-symbol code
+// lengths. False when the lengths over-subscribe the code space; incomplete codes are
+// accepted (an unassigned code then fails at decode time).
+bool huffman_counts(Huffman* h, const uint8_t* lengths, int n) {
   std::memset(h->count, 0, sizeof h->count);
   for (int s = 0; s < n; ++s) h->count[lengths[s]]++;
   h->count[0] = 0;
@@ -76,6 +77,12 @@ bool build_huffman(Huffman* h, const uint8_t* lengths, int n) {
   for (int len = 1; len <= kMaxBits; ++len) offs[len + 1] = offs[len] + h->count[len];
   for (int s = 0; s < n; ++s)
     if (lengths[s]) h->symbol[offs[lengths[s]]++] = static_cast<uint16_t>(s);
+  return true;
+}
+
+// huffman_counts plus the kFast-bit lookup of symbol << 4 | length (the code-length code).
+bool build_huffman(Huffman* h, const uint8_t* lengths, int n) {
+  if (!huffman_counts(h, lengths, n)) return false;
   std::memset(h->fast, 0, sizeof h->fast);
   uint32_t code = 0;
   int idx = 0;
@@ -90,6 +97,85 @@ bool build_huffman(Huffman* h, const uint8_t* lengths, int n) {
   }
   return true;
 }
+
+// Literal/length and distance codes as decode entries: for each kFast-bit lookup, the code
+// length (bits 0-3), the extra-bit count (bits 4-7), the kind (bits 8-9) and the value
+// (bits 16-31: the literal byte, or the base length / distance of RFC 1951 section 3.2.5).
+// An entry of 0 marks a code longer than kFast bits, resolved by the canonical walk.
+enum : uint32_t { kEntLiteral = 0, kEntBase = 1, kEntEnd = 2, kEntBad = 3 };
+constexpr uint16_t kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27,
+                                   31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+constexpr uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                   2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+constexpr uint16_t kDistBase[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129,
+                                    193, 257, 385, 513, 769, 1025, 1537, 2049, 3073,
+                                    4097, 6145, 8193, 12289, 16385, 24577};
+constexpr uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
+                                    6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+
+inline uint32_t make_entry(uint32_t kind, uint32_t value, uint32_t extra, uint32_t len) {
+  return (value << 16) | (kind << 8) | (extra << 4) | len;
+}
+inline uint32_t ent_len(uint32_t e) { return e & 15u; }
+inline uint32_t ent_extra(uint32_t e) { return (e >> 4) & 15u; }
+inline uint32_t ent_kind(uint32_t e) { return (e >> 8) & 3u; }
+inline uint32_t ent_value(uint32_t e) { return e >> 16; }
+
+struct DecodeTable {
+  Huffman h;
+  uint32_t e[1 << kFast];
+  bool dist = false;
+  // The entry of symbol `sym` whose code is `len` bits long.
+  uint32_t entry_of(int sym, uint32_t len) const {
+    if (dist) {
+      if (sym > 29) return make_entry(kEntBad, 0, 0, len);
+      return make_entry(kEntBase, kDistBase[sym], kDistExtra[sym], len);
+    }
+    if (sym < 256) return make_entry(kEntLiteral, static_cast<uint32_t>(sym), 0, len);
+    if (sym == 256) return make_entry(kEntEnd, 0, 0, len);
+    if (sym > 285) return make_entry(kEntBad, 0, 0, len);
+    return make_entry(kEntBase, kLenBase[sym - 257], kLenExtra[sym - 257], len);
+  }
+  // False when the lengths over-subscribe the code space. Each symbol's entry is made once
+  // and replicated over the lookups that start with its (bit-reversed) code.
+  bool build(const uint8_t* lengths, int n, bool is_dist) {
+    dist = is_dist;
+    if (!huffman_counts(&h, lengths, n)) return false;
+    std::memset(e, 0, sizeof e);
+    uint32_t code = 0;
+    int idx = 0;
+    for (int len = 1; len <= kFast; ++len) {
+      for (int k = 0; k < h.count[len]; ++k, ++idx, ++code) {
+        uint32_t rev = 0;
+        for (int b = 0; b < len; ++b) rev |= ((code >> b) & 1u) << (len - 1 - b);
+        const uint32_t x = entry_of(h.symbol[idx], static_cast<uint32_t>(len));
+        for (uint32_t fill = rev; fill < (1u << kFast); fill += 1u << len) e[fill] = x;
+      }
+      code <<= 1;
+    }
+    return true;
+  }
+  // Entry for the next code in `buf` (at least kMaxBits valid bits); a code the table does
+  // not assign gives kEntBad with length 0.
+  uint32_t lookup(uint64_t buf) const {
+    const uint32_t x = e[buf & ((1u << kFast) - 1)];
+    return x ? x : lookup_long(buf);
+  }
+  // Codes longer than kFast bits: the canonical walk (codes of each length are consecutive
+  // integers starting at `first`).
+  __attribute__((noinline)) uint32_t lookup_long(uint64_t buf) const {
+    int code = 0, first = 0, index = 0;
+    for (int len = 1; len <= kMaxBits; ++len) {
+      code |= static_cast<int>((buf >> (len - 1)) & 1);
+      const int count = h.count[len];
+      if (code - first < count) return entry_of(h.symbol[index + code - first], static_cast<uint32_t>(len));
+      index += count;
+      first = (first + count) << 1;
+      code <<= 1;
+    }
+    return make_entry(kEntBad, 0, 0, 0);
+  }
+};
 
 // Bytes that the decoder may write past the end of its output (match copies move 8-byte
 // words); the output buffer must have this many writable bytes after n_out.
@@ -220,14 +306,14 @@ class Inflater {
 
   bool fixed(std::string* why) {
     static const struct Fixed {
-      Huffman lit, dist;
+      DecodeTable lit, dist;
       Fixed() {
         uint8_t l[288];
         for (int s = 0; s < 288; ++s) l[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
-        build_huffman(&lit, l, 288);
+        lit.build(l, 288, false);
         uint8_t d[30];
         std::memset(d, 5, sizeof d);
-        build_huffman(&dist, d, 30);
+        dist.build(d, 30, true);
       }
     } F;
     return codes(F.lit, F.dist, why);
@@ -285,8 +371,8 @@ class Inflater {
       *why = "no end-of-block code";
       return false;
     }
-    Huffman lit, dist;
-    if (!build_huffman(&lit, lengths, nlen) || !build_huffman(&dist, lengths + nlen, ndist)) {
+    DecodeTable lit, dist;
+    if (!lit.build(lengths, nlen, false) || !dist.build(lengths + nlen, ndist, true)) {
       *why = "over-subscribed Huffman code";
       return false;
     }
@@ -294,48 +380,40 @@ class Inflater {
   }
 
   // Literal/length + distance symbols of one compressed block, up to end-of-block (256).
-  bool codes(const Huffman& lit, const Huffman& dist, std::string* why) {
-    static const uint16_t kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27,
-                                          31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
-    static const uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
-                                          2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
-    static const uint16_t kDistBase[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129,
-                                           193, 257, 385, 513, 769, 1025, 1537, 2049, 3073,
-                                           4097, 6145, 8193, 12289, 16385, 24577};
-    static const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
-                                           6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+  bool codes(const DecodeTable& lit, const DecodeTable& dist, std::string* why) {
     for (;;) {
       // One symbol with its match takes at most 15 + 5 + 15 + 13 = 48 bits.
       if (nbits_ < 48) refill();
-      const int sym = decode_buffered(lit);
-      if (sym < 256) {
-        if (sym < 0) {
-          *why = "bad literal/length code";
-          return false;
+      uint32_t e = lit.lookup(buf_);
+      if (ent_kind(e) == kEntLiteral) {
+        if (pos_out_ >= n_out_) return fail(why, "image data longer than the image");
+        consume(ent_len(e));
+        out_[pos_out_++] = static_cast<uint8_t>(ent_value(e));
+        // a second literal needs at most 15 of the >= 33 bits left: no refill
+        e = lit.lookup(buf_);
+        if (ent_kind(e) == kEntLiteral) {
+          if (pos_out_ >= n_out_) return fail(why, "image data longer than the image");
+          consume(ent_len(e));
+          out_[pos_out_++] = static_cast<uint8_t>(ent_value(e));
+          continue;
         }
-        if (pos_out_ >= n_out_) {
-          *why = "image data longer than the image";
-          return false;
+        if (nbits_ < 48) refill();  // the low bits, and so `e`, are unchanged by a refill
+      }
+      if (ent_kind(e) != kEntBase) {
+        if (ent_kind(e) == kEntEnd) {
+          consume(ent_len(e));
+          return true;
         }
-        out_[pos_out_++] = static_cast<uint8_t>(sym);
-        continue;
+        return fail(why, "bad literal/length code");
       }
-      if (sym == 256) return true;
-      if (sym > 285) {
-        *why = "bad length symbol";
-        return false;
-      }
-      const size_t len = kLenBase[sym - 257] + bits_buffered(kLenExtra[sym - 257]);
-      const int dsym = decode_buffered(dist);
-      if (dsym < 0 || dsym > 29) {
-        *why = "bad distance code";
-        return false;
-      }
-      const size_t d = kDistBase[dsym] + bits_buffered(kDistExtra[dsym]);
-      if (d > pos_out_ || len > n_out_ - pos_out_) {
-        *why = d > pos_out_ ? "distance before the start of the data" : "image data longer than the image";
-        return false;
-      }
+      consume(ent_len(e));
+      const size_t len = ent_value(e) + bits_buffered(static_cast<int>(ent_extra(e)));
+      const uint32_t de = dist.lookup(buf_);
+      if (ent_kind(de) != kEntBase) return fail(why, "bad distance code");
+      consume(ent_len(de));
+      const size_t d = ent_value(de) + bits_buffered(static_cast<int>(ent_extra(de)));
+      if (d > pos_out_) return fail(why, "distance before the start of the data");
+      if (len > n_out_ - pos_out_) return fail(why, "image data longer than the image");
       uint8_t* dst = out_ + pos_out_;
       const uint8_t* src = dst - d;
       if (d >= 8) {
@@ -353,11 +431,17 @@ class Inflater {
         for (size_t k = 0; k < len; ++k) dst[k] = src[k];  // overlapping copy repeats the run
       }
       pos_out_ += len;
-      if (overrun()) {
-        *why = "truncated image data";
-        return false;
-      }
+      if (overrun()) return fail(why, "truncated image data");
     }
+  }
+
+  void consume(uint32_t n) {
+    buf_ >>= n;
+    nbits_ -= static_cast<int>(n);
+  }
+  static bool fail(std::string* why, const char* what) {
+    *why = what;
+    return false;
   }
 
   const uint8_t* in_;
