@@ -116,6 +116,16 @@ def test_invalid_args_without_device():
     i = ct.c_int64()
     assert lib.cp_video_windows(10, 1, 0, 1, 5, 0, 0, 0, 0, 0, 1, ct.byref(w), ct.byref(i),
                                 None, None, None, None) == _abi.CP_ERR_ARG
+    # the host-staged multi-setting call checks its arguments before any device work
+    st = _abi.Stack(n=4, width=8, height=8, channels=3, base=None, frame_stride=192)
+    ps = (_abi.Params * 2)()
+    outs = (ct.c_void_p * 2)()
+    assert lib.cp_composite_multi(None, ct.byref(st), ps, 2, outs, None, None) == _abi.CP_ERR_ARG
+    # frame ingest and output encode need no device at all
+    assert lib.cp_load_png(None, None, 1, 0, None, 0, 1, 1, 3) == _abi.CP_ERR_ARG
+    assert lib.cp_save_png(None, b"x.png", None, 1, 1, 3, 6) == _abi.CP_ERR_ARG
+    h, wd, c = ct.c_int32(), ct.c_int32(), ct.c_int32()
+    assert lib.cp_png_info(None, None, ct.byref(wd), ct.byref(h), ct.byref(c)) == _abi.CP_ERR_ARG
 
 
 def test_context_requires_gpu():
