@@ -736,8 +736,9 @@ def run_ingest(args):
     """Frame ingest: the HD stack written as 64 PNG files (Paeth-filtered, zlib level 6),
     decoded by cp_load_png on all host threads into pinned memory, then composited from there
     by cp_composite (abs/0.05/0.2 average): files -> composite, the work the reference does
-    per frame inside its slicing loop (src/streams.rs:63-70). Also reports one-thread decode,
-    the reference's per-frame sequential decode rate."""
+    per frame inside its slicing loop (src/streams.rs:63-70), and the composite and blend
+    mask written back as PNG files by cp_save_png (src/main.rs:519-570): files -> files.
+    Also reports one-thread decode, the reference's per-frame sequential decode rate."""
     import shutil
     import tempfile
     import numpy as np
@@ -788,6 +789,12 @@ def run_ingest(args):
         t0 = time.perf_counter()
         decode(1, n1)
         t_one = (time.perf_counter() - t0) / n1
+        # output encode: the composite and its blend mask as PNG files (zlib level 6)
+        t0 = time.perf_counter()
+        for k, name in enumerate(("composite.png", "blend.png")):
+            ctx.check(lib.cp_save_png(ctx.handle, os.path.join(tmp, name).encode(),
+                                      optr + k * fb, W, H, C, -1), "cp_save_png")
+        t_enc = time.perf_counter() - t0
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     print(json.dumps({
@@ -799,6 +806,11 @@ def run_ingest(args):
                                "decode_ms": 1e3 * t_dec, "composite_e2e_ms": 1e3 * t_comp,
                                "note": "decode, then cp_composite from pinned memory (H2D, "
                                        "kernel, D2H of composite and mask)"},
+        "encode_ms": 1e3 * t_enc,
+        "files_to_files": {"value": MPXF_PER_COMPOSITE / (t_dec + t_comp + t_enc),
+                           "unit": METRIC,
+                           "note": "the above plus cp_save_png of composite and mask, one "
+                                   "thread each, in sequence"},
         "steps": steps, "dtype": "u8", "data": "synthetic (seeded HD stack written as PNG)",
         "config": {"frames": N_FRAMES, "width": W, "height": H, "channels": C,
                    "png": "8-bit RGB, Paeth filter, zlib level 6",
