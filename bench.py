@@ -793,7 +793,7 @@ def run_ingest(args):
         t0 = time.perf_counter()
         for k, name in enumerate(("composite.png", "blend.png")):
             ctx.check(lib.cp_save_png(ctx.handle, os.path.join(tmp, name).encode(),
-                                      optr + k * fb, W, H, C, -1), "cp_save_png")
+                                      optr + k * fb, W, H, C, -1, 0), "cp_save_png")
         t_enc = time.perf_counter() - t0
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
@@ -809,8 +809,8 @@ def run_ingest(args):
         "encode_ms": 1e3 * t_enc,
         "files_to_files": {"value": MPXF_PER_COMPOSITE / (t_dec + t_comp + t_enc),
                            "unit": METRIC,
-                           "note": "the above plus cp_save_png of composite and mask, one "
-                                   "thread each, in sequence"},
+                           "note": "the above plus cp_save_png of composite and mask "
+                                   "(each on all host threads), in sequence"},
         "steps": steps, "dtype": "u8", "data": "synthetic (seeded HD stack written as PNG)",
         "config": {"frames": N_FRAMES, "width": W, "height": H, "channels": C,
                    "png": "8-bit RGB, Paeth filter, zlib level 6",

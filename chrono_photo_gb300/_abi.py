@@ -116,7 +116,7 @@ SIGNATURES = [
     ("cp_server_destroy", ct.c_int, [P]),
     ("cp_png_info", ct.c_int, [P, ct.c_char_p, I32P, I32P, I32P]),
     ("cp_load_png", ct.c_int, [P, ct.POINTER(ct.c_char_p), I32, I32, P, U64, I32, I32, I32]),
-    ("cp_save_png", ct.c_int, [P, ct.c_char_p, P, I32, I32, I32, I32]),
+    ("cp_save_png", ct.c_int, [P, ct.c_char_p, P, I32, I32, I32, I32, I32]),
 ]
 
 _lib = None

@@ -410,16 +410,17 @@ def load_png(paths, threads=0, out=None, context=None):
     return out
 
 
-def save_png(path, image, level=6, context=None):
-    """Writes a uint8 [h, w, c] image (c = 1, 3 or 4) as a PNG file (cp_save_png), creating a
-    missing parent directory like the reference's save_image (src/main.rs:519-570)."""
+def save_png(path, image, level=6, threads=0, context=None):
+    """Writes a uint8 [h, w, c] image (c = 1, 3 or 4) as a PNG file (cp_save_png) on
+    `threads` host threads (0: all), creating a missing parent directory like the reference's
+    save_image (src/main.rs:519-570)."""
     a = np.ascontiguousarray(image, dtype=np.uint8)
     if a.ndim == 2:
         a = a[:, :, None]
     h, w, c = a.shape
     handle = context.handle if context else None
     _check(handle, lib().cp_save_png(handle, str(path).encode(), a.ctypes.data, w, h, c,
-                                     int(level)), "cp_save_png")
+                                     int(level), int(threads)), "cp_save_png")
 
 
 def video_windows(image_count, video_in, video_out=(None, None, 1)):

@@ -14,10 +14,12 @@
 #include <sys/types.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/chrono_gpu.h"
@@ -212,8 +214,14 @@ class Matcher {
   Matcher(const uint8_t* data, size_t n, int level)
       : d_(data), n_(n), e_(effort(level)), head_(1u << kHashBits, -1), prev_(kWindow, -1) {}
 
+  // Makes positions [from, to) available as match sources without coding them (the window
+  // before a segment).
+  void prime(size_t from, size_t to) {
+    for (size_t p = from; p < to && p + kMinMatch <= n_; ++p) insert(p, hash(p));
+  }
+
   // Tokens for [pos, end) appended to `out`; returns the position reached (>= end: a match
-  // may run past `end`).
+  // may run past `end`, never past the matcher's own end n).
   size_t parse(size_t pos, size_t end, std::vector<Token>* out) {
     while (pos < end) {
       int best_len = 0, best_dist = 0;
@@ -429,28 +437,75 @@ void write_block(BitWriter& bw, const std::vector<Token>* tok_list, const uint8_
   bw.put(lcode[256], L[256]);
 }
 
-// zlib stream (RFC 1950) of `data` at `level` (0: stored blocks only).
-std::vector<uint8_t> zlib_encode(const uint8_t* data, size_t n, int level) {
+// Runs fn(0) .. fn(count - 1) on up to `threads` threads (0: all cores), each index once.
+template <typename Fn>
+void run_parallel(size_t count, int threads, Fn fn) {
+  int workers = threads > 0 ? threads : static_cast<int>(std::thread::hardware_concurrency());
+  workers = std::max(1, std::min<int>(workers, static_cast<int>(std::min<size_t>(count, 1024))));
+  std::atomic<size_t> next(0);
+  auto work = [&]() {
+    for (size_t i = next.fetch_add(1); i < count; i = next.fetch_add(1)) fn(i);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < workers; ++t) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+}
+
+// Compressed independently: the filtered data is cut into segments of this many bytes, a
+// fixed size so that the file does not depend on the number of threads.
+constexpr size_t kSegment = 256 * 1024;
+constexpr size_t kBlockTokens = 1u << 15;
+
+// DEFLATE data of data[begin, end) whose matches reach back at most into the 32 KB before
+// `begin`. A segment other than the last ends with an empty stored block (BFINAL 0, LEN 0),
+// which ends it on a byte boundary, so that the segments' bytes concatenate into one stream
+// (the method of parallel gzip).
+std::vector<uint8_t> deflate_segment(const uint8_t* data, size_t begin, size_t end, int level,
+                                     bool last) {
   std::vector<uint8_t> out;
-  out.reserve(n / 2 + 64);
-  out.push_back(0x78);  // deflate, 32 KB window
-  out.push_back(level <= 1 ? 0x01 : level <= 5 ? 0x5E : level == 6 ? 0x9C : 0xDA);
+  out.reserve((end - begin) / 2 + 64);
   BitWriter bw(&out);
-  constexpr size_t kBlockTokens = 1u << 15;
   if (level <= 0) {
-    write_block(bw, nullptr, data, 0, n, true);
+    write_block(bw, nullptr, data, begin, end, last);
   } else {
-    Matcher m(data, n, level);
+    Matcher m(data, end, level);
+    m.prime(begin > static_cast<size_t>(kWindow) ? begin - kWindow : 0, begin);
     std::vector<Token> toks;
-    size_t pos = 0;
-    while (pos < n) {
+    size_t pos = begin;
+    while (pos < end) {
       toks.clear();
-      const size_t begin = pos;
-      while (pos < n && toks.size() < kBlockTokens) pos = m.parse(pos, pos + 1, &toks);
-      write_block(bw, &toks, data, begin, pos, pos >= n);
+      const size_t b = pos;
+      while (pos < end && toks.size() < kBlockTokens) pos = m.parse(pos, pos + 1, &toks);
+      write_block(bw, &toks, data, b, pos, last && pos >= end);
     }
   }
+  if (!last) {
+    bw.put(0, 3);
+    bw.align();
+    bw.put(0, 16);
+    bw.put(0xFFFFu, 16);
+  }
   bw.align();
+  return out;
+}
+
+// zlib stream (RFC 1950) of `data` at `level` (0: stored blocks only), its segments
+// compressed on `threads` threads.
+std::vector<uint8_t> zlib_encode(const uint8_t* data, size_t n, int level, int threads) {
+  const size_t nseg = std::max<size_t>(1, (n + kSegment - 1) / kSegment);
+  std::vector<std::vector<uint8_t>> segs(nseg);
+  run_parallel(nseg, threads, [&](size_t i) {
+    const size_t b = i * kSegment, e = std::min(n, b + kSegment);
+    segs[i] = deflate_segment(data, b, e, level, i + 1 == nseg);
+  });
+  std::vector<uint8_t> out;
+  size_t total = 6;
+  for (const auto& v : segs) total += v.size();
+  out.reserve(total);
+  out.push_back(0x78);  // deflate, 32 KB window
+  out.push_back(level <= 1 ? 0x01 : level <= 5 ? 0x5E : level == 6 ? 0x9C : 0xDA);
+  for (const auto& v : segs) out.insert(out.end(), v.begin(), v.end());
   uint8_t a[4];
   cp::png::put_be32(a, cp::png::adler32(data, n));
   out.insert(out.end(), a, a + 4);
@@ -465,18 +520,17 @@ inline int paeth_pred(int a, int b, int c) {
 }
 inline uint32_t sabs(uint8_t v) { return static_cast<uint32_t>(std::abs(static_cast<int8_t>(v))); }
 
-// Filtered scanlines: per row the filter type (0-4) whose bytes, read as signed, have the
-// smallest sum of absolute values, then the filtered bytes.
-std::vector<uint8_t> filter_rows(const uint8_t* img, int w, int h, int c, bool adaptive) {
+// Rows [y0, y1) of filter_rows into `out` (rows of 1 + stride bytes).
+void filter_band(const uint8_t* img, int w, int c, int y0, int y1, bool adaptive,
+                 const uint8_t* zero, uint8_t* out) {
   const size_t stride = static_cast<size_t>(w) * c;
   const size_t bpp = static_cast<size_t>(c);
-  std::vector<uint8_t> out(static_cast<size_t>(h) * (stride + 1));
-  std::vector<uint8_t> zero(stride, 0), cand[5];
+  std::vector<uint8_t> cand[5];
   for (auto& v : cand) v.resize(stride);
-  for (int y = 0; y < h; ++y) {
+  for (int y = y0; y < y1; ++y) {
     const uint8_t* x = img + static_cast<size_t>(y) * stride;
-    const uint8_t* up = y ? x - stride : zero.data();
-    uint8_t* dst = out.data() + static_cast<size_t>(y) * (stride + 1);
+    const uint8_t* up = y ? x - stride : zero;
+    uint8_t* dst = out + static_cast<size_t>(y) * (stride + 1);
     if (!adaptive) {
       dst[0] = 0;
       std::memcpy(dst + 1, x, stride);
@@ -511,6 +565,21 @@ std::vector<uint8_t> filter_rows(const uint8_t* img, int w, int h, int c, bool a
     dst[0] = static_cast<uint8_t>(best_f);
     std::memcpy(dst + 1, best_f ? cand[best_f].data() : x, stride);
   }
+}
+
+// Filtered scanlines: per row the filter type (0-4) whose bytes, read as signed, have the
+// smallest sum of absolute values, then the filtered bytes. Rows depend only on the image,
+// so bands of rows are filtered in parallel.
+std::vector<uint8_t> filter_rows(const uint8_t* img, int w, int h, int c, bool adaptive,
+                                 int threads) {
+  const size_t stride = static_cast<size_t>(w) * c;
+  std::vector<uint8_t> out(static_cast<size_t>(h) * (stride + 1));
+  const std::vector<uint8_t> zero(stride, 0);
+  constexpr int kBand = 32;
+  run_parallel(static_cast<size_t>((h + kBand - 1) / kBand), threads, [&](size_t band) {
+    const int y0 = static_cast<int>(band) * kBand;
+    filter_band(img, w, c, y0, std::min(h, y0 + kBand), adaptive, zero.data(), out.data());
+  });
   return out;
 }
 
@@ -545,13 +614,14 @@ FILE* open_output(const char* path) {
 }  // namespace
 
 extern "C" int cp_save_png(cp_ctx* ctx, const char* path, const uint8_t* image, int32_t width,
-                           int32_t height, int32_t channels, int32_t level) {
+                           int32_t height, int32_t channels, int32_t level, int32_t threads) {
   if (!path || !image || width < 1 || height < 1 ||
       (channels != 1 && channels != 3 && channels != 4) || level > 9)
     return CP_ERR_ARG;
   if (level < 0) level = 6;
-  const std::vector<uint8_t> rows = filter_rows(image, width, height, channels, level > 0);
-  const std::vector<uint8_t> z = zlib_encode(rows.data(), rows.size(), level);
+  const std::vector<uint8_t> rows = filter_rows(image, width, height, channels, level > 0,
+                                                threads);
+  const std::vector<uint8_t> z = zlib_encode(rows.data(), rows.size(), level, threads);
   std::vector<uint8_t> png;
   png.reserve(z.size() + 128);
   static const uint8_t kSig[8] = {137, 80, 78, 71, 13, 10, 26, 10};

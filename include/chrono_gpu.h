@@ -283,10 +283,11 @@ int cp_load_png(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t thread
 /* Replaces save_image (src/main.rs:519-570: image::save_buffer by file extension, the parent
  * directory created when missing) for PNG output of a composite or blend mask: `image` is
  * height rows of width * channels bytes (1 gray, 3 RGB, 4 RGBA), written losslessly with
- * adaptive scanline filters and zlib `level` 0..9 (0: stored, -1: 6). ctx (nullable)
- * receives the error message; CP_ERR_IO when the file cannot be written. */
+ * adaptive scanline filters and zlib `level` 0..9 (0: stored, -1: 6), compressed in 256 KB
+ * segments on `threads` host threads (0: all cores; the file does not depend on it).
+ * ctx (nullable) receives the error message; CP_ERR_IO when the file cannot be written. */
 int cp_save_png(cp_ctx* ctx, const char* path, const uint8_t* image, int32_t width,
-                int32_t height, int32_t channels, int32_t level);
+                int32_t height, int32_t channels, int32_t level, int32_t threads);
 
 /* ---- serving ------------------------------------------------------------------------- */
 /* A compositing job: a host-memory stack plus options, output buffers in host memory.

@@ -123,7 +123,7 @@ def test_invalid_args_without_device():
     assert lib.cp_composite_multi(None, ct.byref(st), ps, 2, outs, None, None) == _abi.CP_ERR_ARG
     # frame ingest and output encode need no device at all
     assert lib.cp_load_png(None, None, 1, 0, None, 0, 1, 1, 3) == _abi.CP_ERR_ARG
-    assert lib.cp_save_png(None, b"x.png", None, 1, 1, 3, 6) == _abi.CP_ERR_ARG
+    assert lib.cp_save_png(None, b"x.png", None, 1, 1, 3, 6, 0) == _abi.CP_ERR_ARG
     h, wd, c = ct.c_int32(), ct.c_int32(), ct.c_int32()
     assert lib.cp_png_info(None, None, ct.byref(wd), ct.byref(h), ct.byref(c)) == _abi.CP_ERR_ARG
 

@@ -157,3 +157,17 @@ def test_all_block_kinds_are_exercised(tmp_path):
                             for i in _chunk_offsets(d) if d[i + 4:i + 8] == b"IDAT")
             kinds.add((idat[2] >> 1) & 3)  # BTYPE of the first block
     assert kinds == {0, 1, 2}
+
+
+def test_file_independent_of_thread_count(tmp_path):
+    """Segments have a fixed size, so the bytes written do not depend on the threads used;
+    a 1.3 MB image spans several segments (each primed with the 32 KB before it)."""
+    from chrono_photo_gb300 import example_data
+    img = example_data.stack(1, 640, 700, sigma=3, n_disks=2, rmin=20, rmax=40, seed=3)[0]
+    files = []
+    for t in (1, 3, 0):
+        p = str(tmp_path / ("t%d.png" % t))
+        cg.save_png(p, img, level=6, threads=t)
+        files.append(open(p, "rb").read())
+    assert files[0] == files[1] == files[2]
+    assert np.array_equal(cg.load_png([str(tmp_path / "t1.png")])[0], img)
