@@ -206,3 +206,38 @@ def test_image_data_longer_than_the_image(tmp_path):
     _expect_io([p])
     with pytest.raises(cg.ChronoError):
         cg.load_png([str(tmp_path / "missing.png")])
+
+
+def test_damaged_streams_fail_cleanly(tmp_path):
+    """Random damage to the zlib data (bytes flipped, cut, inserted; chunk CRCs kept valid so
+    that the DEFLATE decoder itself meets it): every file either decodes or fails with
+    CP_ERR_IO, never anything else."""
+    rng = np.random.default_rng(11)
+    p = str(tmp_path / "f.png")
+    outcomes = {0: 0, _abi.CP_ERR_IO: 0}
+    for it in range(300):
+        h, w, c = int(rng.integers(1, 30)), int(rng.integers(1, 40)), int(rng.choice([1, 3, 4]))
+        img = (_photo_like(h, w, c, it) if it % 2 else
+               rng.integers(0, 256, size=(h, w, c), dtype=np.uint8))
+
+        def damage(data):
+            b = bytearray(data)
+            kind = int(rng.integers(0, 3))
+            if kind == 0:
+                for _ in range(int(rng.integers(1, 4))):
+                    b[int(rng.integers(0, len(b)))] ^= int(rng.integers(1, 256))
+            elif kind == 1:
+                b = b[:int(rng.integers(0, len(b)))]
+            else:
+                i = int(rng.integers(0, len(b)))
+                b[i:i] = rng.integers(0, 256, size=int(rng.integers(1, 20)), dtype=np.uint8).tobytes()
+            return bytes(b)
+        write_png(p, img, seed=it, level=int(rng.integers(0, 10)),
+                  strategy=int(rng.choice([0, 1, 2, 3, 4])), damage=damage)
+        try:
+            cg.load_png([p])
+            outcomes[0] += 1
+        except cg.ChronoError as e:
+            assert e.status == _abi.CP_ERR_IO, e
+            outcomes[_abi.CP_ERR_IO] += 1
+    assert outcomes[_abi.CP_ERR_IO] > 250
