@@ -316,7 +316,8 @@ typedef struct cp_server cp_server;
 int cp_server_create(cp_ctx* ctx, uint64_t hbm_budget, int32_t max_inflight, cp_server** out);
 /* Non-blocking; the job's buffers must stay valid until it completes. */
 int cp_server_submit(cp_server* srv, const cp_job* job, uint64_t* job_id);
-/* Waits up to timeout_ms (-1 = forever) for job_id. CP_ERR_TIMEOUT if not done yet. */
+/* Waits up to timeout_ms (-1 = forever; 0 = poll without blocking) for job_id.
+ * CP_ERR_TIMEOUT if not done yet. */
 int cp_server_wait(cp_server* srv, uint64_t job_id, int32_t timeout_ms, cp_job_result* res);
 /* Stops accepting jobs, drains the queue and joins the worker. */
 int cp_server_destroy(cp_server* srv);
