@@ -29,6 +29,11 @@ namespace {
 using cp::png::adler32;
 using cp::png::be32;
 using cp::png::crc32_png;
+using cp::png::kCodeLenOrder;
+using cp::png::kDistBase;
+using cp::png::kDistExtra;
+using cp::png::kLenBase;
+using cp::png::kLenExtra;
 
 struct PngHeader {
   int32_t width = 0, height = 0, channels = 0;
@@ -103,16 +108,6 @@ bool build_huffman(Huffman* h, const uint8_t* lengths, int n) {
 // (bits 16-31: the literal byte, or the base length / distance of RFC 1951 section 3.2.5).
 // An entry of 0 marks a code longer than kFast bits, resolved by the canonical walk.
 enum : uint32_t { kEntLiteral = 0, kEntBase = 1, kEntEnd = 2, kEntBad = 3 };
-constexpr uint16_t kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27,
-                                   31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
-constexpr uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
-                                   2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
-constexpr uint16_t kDistBase[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129,
-                                    193, 257, 385, 513, 769, 1025, 1537, 2049, 3073,
-                                    4097, 6145, 8193, 12289, 16385, 24577};
-constexpr uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
-                                    6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
-
 inline uint32_t make_entry(uint32_t kind, uint32_t value, uint32_t extra, uint32_t len) {
   return (value << 16) | (kind << 8) | (extra << 4) | len;
 }
@@ -320,7 +315,6 @@ class Inflater {
   }
 
   bool dynamic(std::string* why) {
-    static const uint8_t kOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
     const int nlen = static_cast<int>(bits(5)) + 257;
     const int ndist = static_cast<int>(bits(5)) + 1;
     const int ncode = static_cast<int>(bits(4)) + 4;
@@ -330,7 +324,7 @@ class Inflater {
     }
     uint8_t lengths[320];
     std::memset(lengths, 0, 19);
-    for (int i = 0; i < ncode; ++i) lengths[kOrder[i]] = static_cast<uint8_t>(bits(3));
+    for (int i = 0; i < ncode; ++i) lengths[kCodeLenOrder[i]] = static_cast<uint8_t>(bits(3));
     Huffman lencode;
     if (!build_huffman(&lencode, lengths, 19)) {
       *why = "bad code-length code";

@@ -1,7 +1,7 @@
-// cp_png.h — checksums of the PNG container shared by the frame reader (cp_ingest.cpp) and
-// the image writer (cp_png_write.cpp): the CRC-32 of every PNG chunk (ISO/IEC 15948, ISO 3309
-// polynomial) and the Adler-32 of the zlib stream (RFC 1950 section 9), plus the big-endian
-// integer helpers of both formats.
+// cp_png.h — what the frame reader (cp_ingest.cpp) and the image writer (cp_png_write.cpp)
+// share: the CRC-32 of every PNG chunk (ISO/IEC 15948, ISO 3309 polynomial), the Adler-32 of
+// the zlib stream (RFC 1950 section 9), the DEFLATE symbol tables (RFC 1951) and the
+// big-endian integer helpers of both formats.
 #pragma once
 
 #include <cstddef>
@@ -69,6 +69,21 @@ inline uint32_t adler32(const uint8_t* p, size_t n) {
 }
 
 inline uint32_t crc32_png(const uint8_t* p, size_t n) { return crc32_update(0, p, n); }
+
+// DEFLATE (RFC 1951 section 3.2.5): base values and extra-bit counts of the 29 length
+// symbols (257..285) and the 30 distance symbols, and the order in which a dynamic block
+// header sends the code lengths of the code-length alphabet (section 3.2.7).
+constexpr uint16_t kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27,
+                                   31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+constexpr uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                   2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+constexpr uint16_t kDistBase[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97, 129,
+                                    193, 257, 385, 513, 769, 1025, 1537, 2049, 3073,
+                                    4097, 6145, 8193, 12289, 16385, 24577};
+constexpr uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
+                                    6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+constexpr uint8_t kCodeLenOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5,
+                                       11, 4, 12, 3, 13, 2, 14, 1, 15};
 
 }  // namespace png
 }  // namespace cp
