@@ -39,14 +39,23 @@ struct PngHeader {
   int32_t width = 0, height = 0, channels = 0;
 };
 
+// The whole file into `data` (one read when the size is known, else in 64 KB pieces).
 bool read_file(const char* path, std::vector<uint8_t>* data) {
   FILE* f = std::fopen(path, "rb");
   if (!f) return false;
   data->clear();
-  uint8_t buf[1 << 16];
-  size_t got;
-  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) data->insert(data->end(), buf, buf + got);
-  const bool ok = !std::ferror(f);
+  long size = -1;
+  if (std::fseek(f, 0, SEEK_END) == 0) size = std::ftell(f);
+  bool ok = std::fseek(f, 0, SEEK_SET) == 0;
+  if (ok && size >= 0) {
+    data->resize(static_cast<size_t>(size));
+    ok = std::fread(data->data(), 1, data->size(), f) == data->size();
+  } else {
+    uint8_t buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) data->insert(data->end(), buf, buf + got);
+    ok = !std::ferror(f);
+  }
   std::fclose(f);
   return ok;
 }
