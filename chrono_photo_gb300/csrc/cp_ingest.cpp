@@ -11,7 +11,10 @@
 // image's; 8-bit gray, RGB and RGBA without interlacing are accepted (the layouts the
 // compositing kernels take), anything else is CP_ERR_IO.
 
+#include <sys/stat.h>
+
 #include <atomic>
+#include <new>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -39,23 +42,15 @@ struct PngHeader {
   int32_t width = 0, height = 0, channels = 0;
 };
 
-// The whole file into `data` (one read when the size is known, else in 64 KB pieces).
+// The whole of a regular file into `data` in one read (anything else, e.g. a directory, is
+// not an image file: false).
 bool read_file(const char* path, std::vector<uint8_t>* data) {
+  struct stat st;
+  if (stat(path, &st) != 0 || !S_ISREG(st.st_mode)) return false;
   FILE* f = std::fopen(path, "rb");
   if (!f) return false;
-  data->clear();
-  long size = -1;
-  if (std::fseek(f, 0, SEEK_END) == 0) size = std::ftell(f);
-  bool ok = std::fseek(f, 0, SEEK_SET) == 0;
-  if (ok && size >= 0) {
-    data->resize(static_cast<size_t>(size));
-    ok = std::fread(data->data(), 1, data->size(), f) == data->size();
-  } else {
-    uint8_t buf[1 << 16];
-    size_t got;
-    while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) data->insert(data->end(), buf, buf + got);
-    ok = !std::ferror(f);
-  }
+  data->resize(static_cast<size_t>(st.st_size));
+  const bool ok = std::fread(data->data(), 1, data->size(), f) == data->size();
   std::fclose(f);
   return ok;
 }
@@ -652,25 +647,39 @@ int decode_png(const char* path, const PngHeader& want, uint8_t* out, Scratch* s
 
 }  // namespace
 
+// Runs an entry point's body so that no C++ exception crosses the C ABI: allocation and
+// thread failures become CP_ERR_OOM with the reason in the context's message.
+template <typename Fn>
+int guarded(cp_ctx* ctx, const char* what, Fn fn) {
+  try {
+    return fn();
+  } catch (const std::exception& e) {
+    cp::ctx_error(ctx, "%s: %s", what, e.what());
+    return CP_ERR_OOM;
+  }
+}
+
 extern "C" int cp_png_info(cp_ctx* ctx, const char* path, int32_t* width, int32_t* height,
                            int32_t* channels) {
   if (!path || !width || !height || !channels) return CP_ERR_ARG;
-  std::vector<uint8_t> data;
-  if (!read_file(path, &data)) {
-    cp::ctx_error(ctx, "cannot read %s", path);
-    return CP_ERR_IO;
-  }
-  PngHeader h;
-  std::string why;
-  const int rc = parse_png(data, &h, nullptr, &why);
-  if (rc) {
-    cp::ctx_error(ctx, "%s: %s", path, why.c_str());
-    return rc;
-  }
-  *width = h.width;
-  *height = h.height;
-  *channels = h.channels;
-  return CP_OK;
+  return guarded(ctx, "cp_png_info", [&]() {
+    std::vector<uint8_t> data;
+    if (!read_file(path, &data)) {
+      cp::ctx_error(ctx, "cannot read %s", path);
+      return CP_ERR_IO;
+    }
+    PngHeader h;
+    std::string why;
+    const int rc = parse_png(data, &h, nullptr, &why);
+    if (rc) {
+      cp::ctx_error(ctx, "%s: %s", path, why.c_str());
+      return rc;
+    }
+    *width = h.width;
+    *height = h.height;
+    *channels = h.channels;
+    return CP_OK;
+  });
 }
 
 extern "C" int cp_load_png(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t threads,
@@ -699,18 +708,32 @@ extern "C" int cp_load_png(cp_ctx* ctx, const char* const* paths, int32_t n, int
     for (;;) {
       const int32_t i = next.fetch_add(1);
       if (i >= n || status.load() != CP_OK) return;
-      const int rc = decode_png(paths[i], want, out + frame_stride * static_cast<uint64_t>(i), &s,
-                                &why);
+      int rc;
+      try {
+        rc = decode_png(paths[i], want, out + frame_stride * static_cast<uint64_t>(i), &s, &why);
+      } catch (const std::exception&) {  // no exception may end a worker thread
+        rc = CP_ERR_OOM;
+        why.clear();
+      }
       if (rc != CP_OK) {
         int expected = CP_OK;
-        if (status.compare_exchange_strong(expected, rc) && !why_taken.test_and_set())
-          first_why = why;
+        if (status.compare_exchange_strong(expected, rc) && !why_taken.test_and_set()) {
+          try {
+            first_why = why.empty() ? std::string(paths[i]) + ": out of host memory" : why;
+          } catch (const std::exception&) {
+          }
+        }
         return;
       }
     }
   };
   std::vector<std::thread> pool;
-  for (int t = 1; t < workers; ++t) pool.emplace_back(work);
+  try {
+    pool.reserve(static_cast<size_t>(workers));
+    for (int t = 1; t < workers; ++t) pool.emplace_back(work);
+  } catch (const std::exception&) {
+    // fewer threads than asked for: the ones started, and this one, share the frames
+  }
   work();
   for (auto& t : pool) t.join();
   if (status.load() != CP_OK) cp::ctx_error(ctx, "%s", first_why.c_str());

@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <new>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -432,18 +433,33 @@ void write_block(BitWriter& bw, const std::vector<Token>* tok_list, const uint8_
 }
 
 // Runs fn(0) .. fn(count - 1) on up to `threads` threads (0: all cores), each index once.
+// An exception in fn stops the remaining work and is rethrown (as std::bad_alloc) on the
+// calling thread after every worker has joined; if fewer threads start than asked for, the
+// started ones share the work.
 template <typename Fn>
 void run_parallel(size_t count, int threads, Fn fn) {
   int workers = threads > 0 ? threads : static_cast<int>(std::thread::hardware_concurrency());
   workers = std::max(1, std::min<int>(workers, static_cast<int>(std::min<size_t>(count, 1024))));
   std::atomic<size_t> next(0);
+  std::atomic<bool> failed(false);
   auto work = [&]() {
-    for (size_t i = next.fetch_add(1); i < count; i = next.fetch_add(1)) fn(i);
+    for (size_t i = next.fetch_add(1); i < count && !failed.load(); i = next.fetch_add(1)) {
+      try {
+        fn(i);
+      } catch (const std::exception&) {
+        failed.store(true);
+      }
+    }
   };
   std::vector<std::thread> pool;
-  for (int t = 1; t < workers; ++t) pool.emplace_back(work);
+  try {
+    pool.reserve(static_cast<size_t>(workers));
+    for (int t = 1; t < workers; ++t) pool.emplace_back(work);
+  } catch (const std::exception&) {
+  }
   work();
   for (auto& t : pool) t.join();
+  if (failed.load()) throw std::bad_alloc();
 }
 
 // Compressed independently: the filtered data is cut into segments of this many bytes, a
@@ -605,13 +621,9 @@ FILE* open_output(const char* path) {
   return std::fopen(path, "wb");
 }
 
-}  // namespace
-
-extern "C" int cp_save_png(cp_ctx* ctx, const char* path, const uint8_t* image, int32_t width,
-                           int32_t height, int32_t channels, int32_t level, int32_t threads) {
-  if (!path || !image || width < 1 || height < 1 ||
-      (channels != 1 && channels != 3 && channels != 4) || level > 9)
-    return CP_ERR_ARG;
+// The body of cp_save_png (which keeps C++ exceptions from crossing the C ABI).
+int save_png(cp_ctx* ctx, const char* path, const uint8_t* image, int32_t width,
+             int32_t height, int32_t channels, int32_t level, int32_t threads) {
   if (level < 0) level = 6;
   const std::vector<uint8_t> rows = filter_rows(image, width, height, channels, level > 0,
                                                 threads);
@@ -643,4 +655,19 @@ extern "C" int cp_save_png(cp_ctx* ctx, const char* path, const uint8_t* image, 
     return CP_ERR_IO;
   }
   return CP_OK;
+}
+
+}  // namespace
+
+extern "C" int cp_save_png(cp_ctx* ctx, const char* path, const uint8_t* image, int32_t width,
+                           int32_t height, int32_t channels, int32_t level, int32_t threads) {
+  if (!path || !image || width < 1 || height < 1 ||
+      (channels != 1 && channels != 3 && channels != 4) || level > 9)
+    return CP_ERR_ARG;
+  try {
+    return save_png(ctx, path, image, width, height, channels, level, threads);
+  } catch (const std::exception& e) {
+    cp::ctx_error(ctx, "cp_save_png: %s", e.what());
+    return CP_ERR_OOM;
+  }
 }

@@ -241,3 +241,14 @@ def test_damaged_streams_fail_cleanly(tmp_path):
             assert e.status == _abi.CP_ERR_IO, e
             outcomes[_abi.CP_ERR_IO] += 1
     assert outcomes[_abi.CP_ERR_IO] > 250
+
+
+def test_directory_is_not_a_frame(tmp_path):
+    """A directory given as a frame path is an I/O error, not a crash."""
+    d = tmp_path / "subdir"
+    d.mkdir()
+    with pytest.raises(cg.ChronoError) as e:
+        cg.png_info(str(d))
+    assert e.value.status == _abi.CP_ERR_IO
+    good = write_png(str(tmp_path / "g.png"), np.zeros((2, 2, 3), np.uint8))
+    _expect_io([good, str(d)])

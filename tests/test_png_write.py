@@ -171,3 +171,9 @@ def test_file_independent_of_thread_count(tmp_path):
         files.append(open(p, "rb").read())
     assert files[0] == files[1] == files[2]
     assert np.array_equal(cg.load_png([str(tmp_path / "t1.png")])[0], img)
+
+
+def test_directory_as_output_path(tmp_path):
+    with pytest.raises(cg.ChronoError) as e:
+        cg.save_png(str(tmp_path), np.zeros((2, 2, 3), np.uint8))
+    assert e.value.status == _abi.CP_ERR_IO
