@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <exception>
 #include <cstring>
 #include <vector>
 
@@ -231,14 +232,26 @@ static int composite_staged(cp_ctx* ctx, const cp_stack* stack, const cp_params*
   return CP_OK;
 }
 
+// composite_staged with no C++ exception crossing the C ABI (host allocations).
+static int composite_guarded(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                             int count, uint8_t* const* outs, uint8_t* const* blends,
+                             const cp_debug* dbg, uint64_t* n_warnings) {
+  try {
+    return composite_staged(ctx, stack, params, count, outs, blends, dbg, n_warnings);
+  } catch (const std::exception& e) {
+    ctx_error(ctx, "host staging: %s", e.what());
+    return CP_ERR_OOM;
+  }
+}
+
 extern "C" int cp_composite(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
                             uint8_t* out, uint8_t* out_blend, const cp_debug* dbg,
                             uint64_t* n_warnings) {
-  return composite_staged(ctx, stack, params, 1, &out, &out_blend, dbg, n_warnings);
+  return composite_guarded(ctx, stack, params, 1, &out, &out_blend, dbg, n_warnings);
 }
 
 extern "C" int cp_composite_multi(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
                                   int32_t count, uint8_t* const* out, uint8_t* const* out_blend,
                                   uint64_t* n_warnings) {
-  return composite_staged(ctx, stack, params, count, out, out_blend, nullptr, n_warnings);
+  return composite_guarded(ctx, stack, params, count, out, out_blend, nullptr, n_warnings);
 }
