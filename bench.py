@@ -14,10 +14,12 @@ Metric: megapixel-frames per second = 6 * 64 * 1920 * 1080 / 1e6 per step / time
               copying the frames again
   roofline    the outlier kernel: algorithmic bytes (n*P*C read + 2*P*C written) per launch /
               its mean launch time, against the measured HBM copy bandwidth
-  cpu_baseline  the C++ restatement of the reference (oracle/) on a band of rows, all cores
+  cpu_baseline  the C++ restatement of the reference (oracle/) on the same whole stack, two
+              steps on all host threads
 
 --impl reference times the reference's CPU algorithm (the oracle restatement; the Rust
-reference cannot be built here) on the same workload and prints its own line.
+reference cannot be built here) on the same workload, the whole stack for every step, and
+prints its own line; it loads the oracle's library only.
 Under torchrun each rank runs the whole workload on its own GPU (replicas, weak scaling).
 """
 import argparse
@@ -217,46 +219,54 @@ def profiled(key):
     return None
 
 
-def cpu_band(rows):
-    from chrono_photo_gb300 import example_data
-    return example_data.hd_stack(seed=2, n=N_FRAMES, w=W, h=rows)
+def example_data_module():
+    """The seeded generators (chrono_photo_gb300/example_data.py, numpy only), loaded from
+    their file so that the reference arm imports nothing else of the package."""
+    import importlib.util
+    path = os.path.join(ROOT, "chrono_photo_gb300", "example_data.py")
+    spec = importlib.util.spec_from_file_location("cp_example_data", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 
-def cpu_sample(threads, frames, reps=1):
-    """Reference CPU path (the oracle's C++ restatement of the reference) on a band of rows of
-    the same stack: the six variants, `reps` times, on `threads` host threads.
-    Returns (Mpx-frames/s, seconds, description)."""
-    from chrono_photo_gb300 import make_params
+def reference_settings():
+    """The six settings as cp_params built by the oracle's pure-Python option parser."""
     from oracle import oracle
-    rows = frames.shape[1]
-    keep = []
-    params = [make_params(keep=keep, **kw) for _, kw in VARIANTS]
+    return [oracle.params(**kw) for _, kw in VARIANTS]
+
+
+def cpu_step(frames, settings, threads):
+    """One step on the CPU: the reference's algorithm (the oracle's C++ restatement) for the
+    six settings on the whole stack, `threads` host threads. Returns seconds."""
+    from oracle import oracle
     t0 = time.perf_counter()
-    for _ in range(reps):
-        for p in params:
-            oracle.composite(frames, p, threads=threads)
-    dt = time.perf_counter() - t0
-    mpxf = reps * len(VARIANTS) * N_FRAMES * W * rows / 1e6
-    return mpxf / dt, dt, "%d x 6 variants on a 64x1920x%d band (%d rows of 1080), %d threads" % (
-        reps, rows, rows, threads)
+    for p in settings:
+        oracle.composite(frames, p, threads=threads)
+    return time.perf_counter() - t0
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU algorithm on the machine's host cores, the same
+    64 x 1920x1080 stack and six settings per step as the GPU arm, `--warmup` untimed and
+    `--steps` timed steps. Only the oracle's library is loaded (no library of the product)."""
     ws, rank = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    frames = cpu_band(160)   # one step: the six variants on 160 rows (~0.25 s on 16 cores)
+    frames = example_data_module().hd_stack(seed=2)
+    settings = reference_settings()
     for _ in range(args.warmup):
-        cpu_sample(threads, frames)
+        cpu_step(frames, settings, threads)
     t = 0.0
     for _ in range(args.steps):
-        v, dt, desc = cpu_sample(threads, frames)
-        t += dt
-    value = args.steps * len(VARIANTS) * N_FRAMES * W * 160 / 1e6 / t
+        t += cpu_step(frames, settings, threads)
+    value = args.steps * len(VARIANTS) * MPXF_PER_COMPOSITE / t
+    desc = ("the whole 64x1920x1080 stack, six settings per step, %d timed steps, %d threads"
+            % (args.steps, threads))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * len(VARIANTS) * MPXF_PER_COMPOSITE / value,
+            "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded)", "config": CONFIG,
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
@@ -394,7 +404,12 @@ def run_gpu(args):
         issue = {"achieved": ach, "peak": issue_peak, "unit": "G warp instructions/s",
                  "frac": ach / issue_peak, "kernel": "k_composite<3, 1, 2, 1> (abs average)",
                  "instructions_per_launch": instr}
-    cpu_v, cpu_dt, cpu_desc = cpu_sample(os.cpu_count() or 1, cpu_band(320), reps=3)
+    # the reference's CPU algorithm on the same whole stack: two steps on all host threads
+    cpu_threads = os.cpu_count() or 1
+    cpu_settings = reference_settings()
+    cpu_t = sum(cpu_step(host, cpu_settings, cpu_threads) for _ in range(2))
+    cpu_v = 2 * len(VARIANTS) * MPXF_PER_COMPOSITE / cpu_t
+    cpu_desc = "2 steps (six settings on the whole 64x1920x1080 stack), %d threads" % cpu_threads
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
@@ -415,7 +430,7 @@ def run_gpu(args):
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "kernel": "k_composite<3> (outlier)", "peak_kind": peak_kind},
         "issue_roofline": issue,
-        "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": os.cpu_count(),
+        "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cpu_threads,
                          "kind": "port", "sample": cpu_desc},
         "clocks": clk_summary,
         "gpu_launches": args.steps * len(VARIANTS),

@@ -1,13 +1,106 @@
 """ctypes binding of the CPU oracle (oracle/chrono_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: the parity checker of the test suite and the smoke check, and the
-timed CPU baseline of bench.py. The product library never imports it.
+timed CPU baseline of bench.py. The product library never imports it, and it imports nothing
+of the product: the option and stack structs below are its own ctypes copies of the plain C
+layouts that include/chrono_gpu.h declares (tests/test_abi.py checks that they match), and
+`params()` builds the parsed options in Python, so a process that only runs the oracle maps
+liboracle.so and no other library of this repository.
 """
 import ctypes as ct
 import os
 import subprocess
 
 import numpy as np
+
+MODE = {"outlier": 0, "darker": 1, "lighter": 2}
+OUTLIER = {"first": 0, "last": 1, "extreme": 2, "average": 3, "forward": 4, "backward": 5}
+BACKGROUND = {"first": 0, "random": 1, "average": 2, "median": 3}
+
+
+class Fade(ct.Structure):
+    """cp_fade."""
+    _fields_ = [("enabled", ct.c_int32), ("repeat", ct.c_int32), ("absolute", ct.c_int32),
+                ("n_points", ct.c_int32), ("frames", ct.POINTER(ct.c_int32)),
+                ("values", ct.POINTER(ct.c_float))]
+
+
+class Params(ct.Structure):
+    """cp_params: the parsed CLI options of one composite."""
+    _fields_ = [("mode", ct.c_int32), ("thr_abs", ct.c_int32), ("thr_min", ct.c_float),
+                ("thr_max", ct.c_float), ("outlier", ct.c_int32), ("background", ct.c_int32),
+                ("weights", ct.c_float * 4), ("fade", Fade),
+                ("sample", ct.POINTER(ct.c_int32)), ("n_sample", ct.c_int32),
+                ("rng_seed", ct.c_uint64)]
+
+
+class Stack(ct.Structure):
+    """cp_stack."""
+    _fields_ = [("n", ct.c_int32), ("width", ct.c_int32), ("height", ct.c_int32),
+                ("channels", ct.c_int32), ("frames", ct.POINTER(ct.c_void_p)),
+                ("base", ct.c_void_p), ("frame_stride", ct.c_int64),
+                ("crop", ct.POINTER(ct.c_int32)), ("src_width", ct.c_int32),
+                ("src_height", ct.c_int32), ("frame_offset", ct.c_int32)]
+
+
+class Debug(ct.Structure):
+    """cp_debug."""
+    _fields_ = [("median", ct.c_void_p), ("q1", ct.c_void_p), ("q3", ct.c_void_p),
+                ("outlier_bits", ct.c_void_p), ("chosen", ct.c_void_p),
+                ("background", ct.c_void_p), ("n_outliers", ct.c_void_p)]
+
+
+def params(mode="outlier", threshold="abs/0.05/0.2", outlier="extreme", background="random",
+           weights=(1.0, 1.0, 1.0, 1.0), fade=None, sample=None, seed=0x5EED):
+    """The parsed options of the reference's CLI as a cp_params, built in Python: defaults of
+    src/cli.rs:192-216 (outlier, abs/0.05/0.2, background random, extreme, weights 1 1 1 1,
+    no fade); `threshold` is "(abs|rel)/min[/max]" with max defaulting to min
+    (src/options.rs:270-276); `fade` is "(clamp|repeat)/(abs|rel)/f,v/..." (src/options.rs:
+    141-187). The buffers the struct points into travel on it as `_keep`."""
+    p = Params()
+    keep = []
+    parts = threshold.split("/")
+    if parts[0] not in ("abs", "absolute", "rel", "relative") or len(parts) < 2:
+        raise ValueError("threshold must be (abs|rel)/min[/max]: %r" % threshold)
+    p.mode = MODE[mode]
+    p.thr_abs = 1 if parts[0].startswith("abs") else 0
+    p.thr_min = float(parts[1])
+    p.thr_max = float(parts[2]) if len(parts) > 2 else float(parts[1])
+    p.outlier = OUTLIER[outlier]
+    p.background = BACKGROUND[background]
+    w = list(weights) + [1.0] * (4 - len(weights))
+    for i in range(4):
+        p.weights[i] = float(w[i])
+    p.fade.absolute = 1  # FadeMode default of an absent --fade (unused while disabled)
+    if fade:
+        fp = fade.split("/")
+        if fp[0] not in ("clamp", "repeat") or fp[1] not in ("abs", "absolute", "rel", "relative"):
+            raise ValueError("fade must be (clamp|repeat)/(abs|rel)/f,v/...: %r" % fade)
+        pts = [(int(a), float(b)) for a, b in (q.split(",") for q in fp[2:])]
+        fr = (ct.c_int32 * len(pts))(*[a for a, _ in pts])
+        va = (ct.c_float * len(pts))(*[b for _, b in pts])
+        keep += [fr, va]
+        p.fade.enabled = 1
+        p.fade.repeat = 1 if fp[0] == "repeat" else 0
+        p.fade.absolute = 1 if fp[1].startswith("abs") else 0
+        p.fade.n_points = len(pts)
+        p.fade.frames = ct.cast(fr, ct.POINTER(ct.c_int32))
+        p.fade.values = ct.cast(va, ct.POINTER(ct.c_float))
+    if sample is not None and len(sample) > 0:
+        arr = (ct.c_int32 * len(sample))(*[int(s) for s in sample])
+        keep.append(arr)
+        p.sample = ct.cast(arr, ct.POINTER(ct.c_int32))
+        p.n_sample = len(sample)
+    p.rng_seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    p._keep = keep
+    return p
+
+
+def _addr(s):
+    """Address of a ctypes struct: the oracle takes the C layouts by pointer, whichever
+    Python class (this module's or the product binding's) describes them."""
+    return None if s is None else ct.addressof(s)
+
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
@@ -32,7 +125,6 @@ def lib():
     global _lib
     if _lib is None:
         build()
-        from chrono_photo_gb300 import _abi
         l = ct.CDLL(LIB)
         P = ct.c_void_p
         l.or_quartiles.argtypes = [P, ct.c_int32, ct.POINTER(ct.c_float), ct.POINTER(ct.c_float),
@@ -45,9 +137,8 @@ def lib():
         l.or_blend_into_u8.argtypes = [P, P, ct.c_int32, ct.c_float]
         l.or_gen_range.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint32]
         l.or_gen_range.restype = ct.c_uint32
-        l.or_fade_lut.argtypes = [ct.POINTER(_abi.Fade), ct.c_int32, ct.c_int32, ct.POINTER(ct.c_float)]
-        l.or_composite.argtypes = [ct.POINTER(_abi.Stack), ct.POINTER(_abi.Params), P, P,
-                                   ct.POINTER(_abi.Debug), ct.POINTER(ct.c_uint64), ct.c_int32]
+        l.or_fade_lut.argtypes = [P, ct.c_int32, ct.c_int32, ct.POINTER(ct.c_float)]
+        l.or_composite.argtypes = [P, P, P, P, P, ct.POINTER(ct.c_uint64), ct.c_int32]
         l.or_shake_analyze.argtypes = [ct.POINTER(P), ct.c_int32, ct.c_int32, ct.c_int32,
                                        ct.c_int32, P, ct.c_int32, ct.c_int32, ct.c_int32, P, P,
                                        ct.c_int32]
@@ -56,6 +147,14 @@ def lib():
                                                            ct.POINTER(ct.c_int64), P, P, P, P]
         _lib = l
     return _lib
+
+
+def fade_lut(fade, n, frame_offset=0):
+    """fade(i, n, frame_offset) of every sample from a cp_fade struct."""
+    o = (ct.c_float * n)()
+    if lib().or_fade_lut(_addr(fade), n, frame_offset, o) != 0:
+        raise ValueError("invalid fade")
+    return np.frombuffer(o, np.float32).copy()
 
 
 def quartiles(sorted_values):
@@ -70,10 +169,9 @@ def quartiles(sorted_values):
 def composite(frames, params, frame_offset=0, crop=None, out_size=None, threads=1, debug=False):
     """OutlierProcessor / SimpleProcessor restated on the CPU. frames: uint8 [n, h, w, c].
     Returns (composite, blend mask, warnings[, debug dict])."""
-    from chrono_photo_gb300 import _abi
     a = np.ascontiguousarray(frames, dtype=np.uint8)
     n, h, w, c = a.shape
-    st = _abi.Stack()
+    st = Stack()
     st.n, st.channels = n, c
     st.base = a.ctypes.data
     st.frame_stride = h * w * c
@@ -98,10 +196,10 @@ def composite(frames, params, frame_offset=0, crop=None, out_size=None, threads=
                   "outlier_bits": np.zeros((h, w, words), np.uint32),
                   "chosen": np.zeros((h, w), np.int32), "background": np.zeros((h, w), np.int32),
                   "n_outliers": np.zeros((h, w), np.int32)}
-        dbg = _abi.Debug(*[arrays[k].ctypes.data for k in ("median", "q1", "q3", "outlier_bits",
+        dbg = Debug(*[arrays[k].ctypes.data for k in ("median", "q1", "q3", "outlier_bits",
                                                             "chosen", "background", "n_outliers")])
-    rc = lib().or_composite(ct.byref(st), ct.byref(params), out.ctypes.data, blend.ctypes.data,
-                            ct.byref(dbg) if dbg is not None else None, ct.byref(warn), threads)
+    rc = lib().or_composite(_addr(st), _addr(params), out.ctypes.data, blend.ctypes.data,
+                            _addr(dbg), ct.byref(warn), threads)
     if rc != 0:
         raise ValueError("oracle rejected the stack (%d)" % rc)
     if debug:

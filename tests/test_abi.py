@@ -46,6 +46,41 @@ def test_struct_sizes_match_c_layout():
     assert ct.sizeof(_abi.Stack) == 16 + 8 + 8 + 8 + 8 + 16
 
 
+def test_oracle_structs_match_binding():
+    """The oracle's own copies of the C layouts (it imports nothing of the product) match the
+    product binding field by field: same names, types, offsets and sizes."""
+    for a, b in ((oracle.Fade, _abi.Fade), (oracle.Params, _abi.Params),
+                 (oracle.Stack, _abi.Stack), (oracle.Debug, _abi.Debug)):
+        assert ct.sizeof(a) == ct.sizeof(b)
+        assert [f for f, _ in a._fields_] == [f for f, _ in b._fields_]
+        for (name, _), _x in zip(a._fields_, b._fields_):
+            assert getattr(a, name).offset == getattr(b, name).offset
+            assert getattr(a, name).size == getattr(b, name).size
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(mode="darker"), dict(mode="lighter", weights=(1, 0.5)),
+                                dict(threshold="rel/3/6", outlier="average", background="first"),
+                                dict(threshold="abs/0.1", fade="clamp/rel/0,1/4,0", weights=(1, 0, 2)),
+                                dict(sample=[0, 2, 5], seed=7, outlier="backward")])
+def test_oracle_params_match_make_params(kw):
+    """oracle.params (pure Python, used by the benchmark's reference arm) builds the same
+    cp_params as the product's make_params; pointer fields are compared by what they hold."""
+    a = oracle.params(**kw)
+    b = cases.params(**kw)
+
+    def strip(p):
+        q = oracle.Params.from_buffer_copy(bytes(p))
+        q.fade.frames = None
+        q.fade.values = None
+        q.sample = None
+        return bytes(q)
+    assert strip(a) == strip(b)
+    n = a.fade.n_points
+    assert [a.fade.frames[i] for i in range(n)] == [b.fade.frames[i] for i in range(n)]
+    assert [a.fade.values[i] for i in range(n)] == [b.fade.values[i] for i in range(n)]
+    assert [a.sample[i] for i in range(a.n_sample)] == [b.sample[i] for i in range(b.n_sample)]
+
+
 def test_version_and_status():
     lib = cg.lib()
     assert b"sm_103a" in lib.cp_version()
@@ -72,9 +107,7 @@ def test_fade_lut_matches_reference(spec, n, offset):
     assert np.array_equal(got, want)
     keep = []
     c = fd.to_c(keep)
-    o = (ct.c_float * n)()
-    assert oracle.lib().or_fade_lut(ct.byref(c), n, offset, o) == 0
-    assert np.array_equal(np.frombuffer(o, np.float32), want)
+    assert np.array_equal(oracle.fade_lut(c, n, offset), want)
 
 
 def test_video_windows_match_oracle():
