@@ -108,6 +108,7 @@ SIGNATURES = [
                                              ct.POINTER(P), P, P]),
     ("cp_composite_batch_static", ct.c_int, [ct.POINTER(Stack), ct.POINTER(Params), I32,
                                              ct.POINTER(P), ct.POINTER(P), P, P]),
+    ("cp_composite_batch_static_status", ct.c_int, [I32P, P]),
     ("cp_shake_analyze_device", ct.c_int, [P, ct.POINTER(P), I32, I32, I32, I32, I32P, I32,
                                            I32, I32, I32P, I32P]),
     ("cp_server_create", ct.c_int, [P, U64, I32, ct.POINTER(P)]),

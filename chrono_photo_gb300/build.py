@@ -6,6 +6,7 @@ chrono_photo_gb300/lib/libchrono_gpu.so.
 """
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -58,12 +59,31 @@ def _run(cmd):
     return p.stdout
 
 
+def _arch_stamp():
+    """Objects and the library built on another host architecture (a copied tree) are
+    rebuilt: the stamp records the machine they were built for."""
+    stamp = os.path.join(OBJ_DIR, "HOST_ARCH")
+    here = platform.machine()
+    try:
+        same = open(stamp).read().strip() == here
+    except OSError:
+        same = False
+    if not same:
+        for d in (OBJ_DIR, LIB_DIR):
+            for f in os.listdir(d):
+                if f.endswith((".o", ".so", ".tmp")):
+                    os.remove(os.path.join(d, f))
+        with open(stamp, "w") as f:
+            f.write(here + "\n")
+
+
 def build(verbose=False, jobs=None):
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     cxx = os.environ.get("CXX", "g++")
     os.makedirs(LIB_DIR, exist_ok=True)
     os.makedirs(OBJ_DIR, exist_ok=True)
+    _arch_stamp()
     hdrs = [os.path.join(CSRC, h) for h in HEADERS]
     hdrs.append(os.path.join(HERE, "..", "include", "chrono_gpu.h"))
     steps, objs = [], []

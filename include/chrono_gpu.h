@@ -235,22 +235,28 @@ int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* frames, int32_t
                               const cp_params* params, uint8_t* const* outs,
                               uint8_t* const* out_blends, uint64_t* warnings, void* stream);
 
-/* Allocation-free form of cp_composite_batch_device, for callers that cannot call
- * cudaMalloc (code running while a CUDA graph is captured, plug-ins whose host owns all
- * device memory, services with a fixed footprint). No counterpart in the reference. It needs
- * no context: it runs on the current device and stream `stream`, and keeps its scratch
- * (stack descriptors, tile prefix sums, work counter) in one fixed __device__ array of
- * about 190 KB that every GPU loading the library holds until exit. At most
- * CP_STATIC_MAX_STACKS stacks per call (more: CP_ERR_LIMIT). The first call on a device
- * looks up the array's device address; make that first call before any stream capture.
- * All calls share the array, so calls that overlap on the GPU (other streams, other host
- * threads) race: order them on one stream. Inputs, outputs and warnings (device array of
- * n_stacks counters, nullable) are as for cp_composite_batch_device; the launch is not
- * graph-cached. Asynchronous. */
+/* Allocation-free form of cp_composite_batch_device. No counterpart in the reference. For
+ * callers that cannot call cudaMalloc: a plug-in inside a host application whose own
+ * allocator owns all device memory, or a service that must not grow its device footprint
+ * after start-up. It needs no context: it runs on the current device and on `stream`, and
+ * keeps its scratch (stack descriptors, tile prefix sums, work counter, error flag) in one
+ * fixed __device__ array of about 190 KB that every GPU loading the library holds until the
+ * process exits. At most CP_STATIC_MAX_STACKS stacks per call (more: CP_ERR_LIMIT). The
+ * first call on a device (with that device current) looks up the array's device address;
+ * the address is kept for the life of the process, so a cudaDeviceReset() followed by more
+ * calls is not supported. The descriptors are passed to the GPU as kernel parameters, so
+ * the call returns without waiting for earlier work on `stream`. All calls share the array:
+ * calls that overlap on the GPU (other streams, other host threads) race, so order them on
+ * one stream. Inputs, outputs and warnings (device array of n_stacks counters, nullable)
+ * are as for cp_composite_batch_device. */
 #define CP_STATIC_MAX_STACKS 64
 int cp_composite_batch_static(const cp_stack* stacks, const cp_params* params, int32_t n_stacks,
                               uint8_t* const* outs, uint8_t* const* out_blends,
                               uint64_t* warnings, void* stream);
+/* Device-side status of the last cp_composite_batch_static call on the current device:
+ * waits for `stream`, then *status = CP_OK, or CP_ERR_TIMEOUT when a tile's bounded wait
+ * for its staged frames gave up (that call's outputs are incomplete). Allocates nothing. */
+int cp_composite_batch_static_status(int32_t* status, void* stream);
 
 /* ---- camera shake -------------------------------------------------------------------- */
 /* ShakeAnalyzer::analyze (src/shake.rs:190-313): anchor windows of radius anchor_radius
@@ -311,8 +317,10 @@ typedef struct cp_job_result {
 
 typedef struct cp_server cp_server;
 /* max_inflight: jobs whose work may be on the device at once. The server admits jobs
- * against the context's HBM budget (hbm_budget, 0 = the context's) as memory frees up and
- * merges the tiles of all admitted jobs into the running persistent launches. */
+ * against the context's HBM budget (hbm_budget, 0 = the context's) as memory frees up,
+ * uploads each admitted job's frames on copy streams, and launches the jobs whose uploads
+ * have landed together in one batched persistent launch per channel count, on rotating
+ * compute streams, so that new launches overlap the ones still running. */
 int cp_server_create(cp_ctx* ctx, uint64_t hbm_budget, int32_t max_inflight, cp_server** out);
 /* Non-blocking; the job's buffers must stay valid until it completes. */
 int cp_server_submit(cp_server* srv, const cp_job* job, uint64_t* job_id);

@@ -66,6 +66,24 @@ def small():
     return example_data.small_stack(seed=1, scale=2)
 
 
+@pytest.fixture(scope="module")
+def small_full():
+    """The small-stack configuration at its stated size: 16 frames of 640x480 (seed 1)."""
+    return example_data.small_stack(seed=1, scale=1)
+
+
+@pytest.mark.parametrize("kw", [
+    dict(threshold="abs/0.05/0.2", outlier="extreme", background="first"),
+    dict(threshold="abs/0.05/0.2", outlier="extreme", background="random", seed=3),
+    dict(threshold="abs/0.05/0.2", outlier="average", background="average"),
+    dict(threshold="rel/3/6", outlier="forward", background="median")],
+    ids=["extreme-first", "extreme-random", "average-average", "rel-forward-median"])
+def test_config1_full_size(ctx, small_full, kw):
+    """16 x 640x480, abs/0.05/0.2 extreme (the configuration's own settings) and three other
+    settings, against the oracle on the whole frame: every debug output bit-exact."""
+    compare(ctx, small_full, mode="outlier", **kw)
+
+
 @pytest.mark.parametrize("outlier", OUTLIERS)
 def test_small_stack_outlier_modes(ctx, small, outlier):
     compare(ctx, small, mode="outlier", threshold="abs/0.05/0.2", outlier=outlier,
@@ -105,8 +123,9 @@ def test_frame_counts(ctx, n):
 @pytest.mark.parametrize("c", [1, 3, 4])
 @pytest.mark.parametrize("n", [33, 48, 64])
 def test_rel_33_to_64_frames(ctx, n, c):
-    """Rel thresholds on 33..64 frames take the sorting-network order statistics: quartiles,
-    medians and their successors for every channel count, with weights and a subsample."""
+    """Rel thresholds on 33..64 frames: the radix selections over two 32-frame plane words
+    give quartiles, medians and their successors for every channel count, with weights and
+    a subsample (the sample mask is the selections' initial candidate set)."""
     rng = np.random.default_rng(300 + n * 10 + c)
     frames = cases.random_stack(rng, n, 11, 45, c, n_spots=5)
     compare(ctx, frames, mode="outlier", threshold="rel/2/4", outlier="extreme",

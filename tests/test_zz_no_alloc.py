@@ -1,10 +1,12 @@
 """The allocation-free batched entry point, cp_composite_batch_static (needs a GB300).
 
-It exists for callers that cannot call cudaMalloc (graph capture in progress, a host
-application that owns all device memory, a fixed footprint): its scratch is a fixed device
-array inside the library. Its output must equal cp_composite_batch_device's on the same
-inputs, on two calls in a row (the second call finds the previous call's scratch contents).
-The test allocates its own inputs and outputs; the entry point allocates nothing."""
+It exists for callers that cannot call cudaMalloc (a plug-in whose host application's
+allocator owns all device memory, a service with a fixed device footprint): its scratch is a
+fixed device array inside the library. Its output must equal cp_composite_batch_device's on
+the same inputs, and the oracle's, on two calls in a row (the second call finds the previous
+call's scratch contents), and its status query must report that every bounded wait
+completed. The test allocates its own inputs and outputs; the entry point allocates
+nothing."""
 import ctypes as ct
 
 import numpy as np
@@ -12,6 +14,7 @@ import pytest
 
 import chrono_photo_gb300 as cg
 from chrono_photo_gb300 import _abi
+from oracle import oracle
 from tests import cases
 
 pytestmark = pytest.mark.gpu
@@ -34,6 +37,7 @@ def test_static_batch_equals_batch_device(ctx):
         outs = {k: (ct.c_void_p * n_st)() for k in ("dev", "st")}
         blends = {k: (ct.c_void_p * n_st)() for k in ("dev", "st")}
         shapes = []
+        oracle_out = []
         for i, (n, h, w, kw) in enumerate(specs):
             frames = cases.random_stack(rng, n, h, w, 3, n_spots=5)
             base = ctx.upload(frames)
@@ -41,6 +45,7 @@ def test_static_batch_equals_batch_device(ctx):
             stacks[i] = _abi.Stack(n=n, width=w, height=h, channels=3, base=base,
                                    frame_stride=h * w * 3, frame_offset=i)
             params[i] = cg.make_params(keep=keep, **kw)
+            oracle_out.append(oracle.composite(frames, params[i], frame_offset=i))
             for k in ("dev", "st"):
                 outs[k][i] = ctx.alloc(h * w * 3)
                 blends[k][i] = ctx.alloc(h * w * 3)
@@ -65,13 +70,23 @@ def test_static_batch_equals_batch_device(ctx):
                                                       blends["st"], warn["st"], stream)
             assert rc == _abi.CP_OK, "call %d: %d" % (call, rc)
             ctx.synchronize()
+            status = ct.c_int32(-99)
+            assert _abi.lib().cp_composite_batch_static_status(ct.byref(status), stream) == 0
+            assert status.value == _abi.CP_OK
             for i, s in enumerate(shapes):
-                cases.assert_close_u8(ctx.download(outs["st"][i], s), ref[i][0],
-                                      what="call %d composite %d" % (call, i))
+                got = ctx.download(outs["st"][i], s)
+                cases.assert_close_u8(got, ref[i][0], what="call %d composite %d" % (call, i))
+                cases.assert_close_u8(got, oracle_out[i][0],
+                                      what="call %d composite %d vs oracle" % (call, i))
                 if specs[i][3]["mode"] == "outlier":
-                    cases.assert_close_u8(ctx.download(blends["st"][i], s), ref[i][1],
-                                          what="call %d blend %d" % (call, i))
-            assert np.array_equal(ctx.download(warn["st"], (n_st,), np.uint64), ref_warn)
+                    gb = ctx.download(blends["st"][i], s)
+                    cases.assert_close_u8(gb, ref[i][1], what="call %d blend %d" % (call, i))
+                    cases.assert_close_u8(gb, oracle_out[i][1],
+                                          what="call %d blend %d vs oracle" % (call, i))
+            got_warn = ctx.download(warn["st"], (n_st,), np.uint64)
+            assert np.array_equal(got_warn, ref_warn)
+            assert [int(x) for x in got_warn] == [o[2] if specs[i][3]["mode"] == "outlier" else 0
+                                                  for i, o in enumerate(oracle_out)]
     finally:
         for p in ptrs:
             ctx.free(p)
