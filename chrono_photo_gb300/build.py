@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-f
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
 CU_SOURCES = ["cp_kernels_c3.cu", "cp_kernels_c4.cu", "cp_kernels_c1.cu", "cp_shake.cu",
-              "cp_static.cu"]
+              "cp_static.cu", "cp_video.cu"]
 # cp_kernels_variant.cu compiled once per specialised single-stack outlier kernel:
 # (channels, distance kind, outlier group, background), the CP_VARIANTS list of cp_internal.h
 KERNEL_VARIANTS = [(3, k, g, b) for k in (1, 2) for b in (1, 0) for g in (1, 2, 3)] + \

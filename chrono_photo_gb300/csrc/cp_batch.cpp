@@ -10,8 +10,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "../../include/chrono_gpu.h"
@@ -259,6 +262,118 @@ extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
                    stream);
 }
 
+// Windows that slide by one frame over a sequence of resident frames (chrono-video with
+// step 1: every window of the steady middle part of create_video, src/main.rs:230-286) run
+// the sliding kernel (cp_video.cu) when the options allow it: RGB, outlier mode with an abs
+// threshold and 0/1 weights (integer distances), no fade, no --sample, 16-byte aligned
+// frames. Each maximal run of at least kMinSlideRun windows of one length 2..CP_MAX_FRAMES,
+// each window the previous one shifted by one frame, is one run; done[k] marks the windows
+// handled here, the rest (the growing and shrinking windows at the ends) go to the batched
+// kernel.
+static constexpr int kMinSlideRun = 3;
+
+static int video_sliding(cp_ctx* ctx, const uint8_t* const* frames, int32_t image_count,
+                         int32_t width, int32_t height, int32_t channels, int32_t n_windows,
+                         const int64_t* win_start, const int32_t* win_len,
+                         const int32_t* win_indices, const cp_params* params,
+                         uint8_t* const* outs, uint8_t* const* out_blends, uint64_t* warnings,
+                         void* stream, std::vector<char>& done) {
+  if (channels != 3 || params->mode != CP_MODE_OUTLIER || !params->thr_abs ||
+      params->fade.enabled || (params->sample && params->n_sample > 0))
+    return CP_OK;
+  for (int i = 0; i < 3; ++i)
+    if (!(params->weights[i] == 0.0f || params->weights[i] == 1.0f)) return CP_OK;
+  const int og = outlier_group(params->outlier);
+  const int bg_first = params->background == CP_BG_FIRST ? 1 : 0;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  auto aligned = [&](int k) {
+    for (int i = 0; i < win_len[k]; ++i)
+      if (reinterpret_cast<uintptr_t>(frames[win_indices[win_start[k] + i]]) & 15) return false;
+    return true;
+  };
+  auto slides = [&](int k) {  // window k is window k - 1 shifted by one frame
+    const int L = win_len[k];
+    if (win_len[k - 1] != L) return false;
+    for (int i = 0; i + 1 < L; ++i)
+      if (win_indices[win_start[k - 1] + i + 1] != win_indices[win_start[k] + i]) return false;
+    return true;
+  };
+  std::unique_ptr<VideoArgs> args;
+  int k = 0;
+  while (k < n_windows) {
+    const int L = win_len[k];
+    if (L < 2 || L > CP_MAX_FRAMES || !aligned(k)) {
+      ++k;
+      continue;
+    }
+    int e = k + 1;
+    while (e < n_windows && slides(e) && aligned(e)) ++e;
+    if (e - k < kMinSlideRun) {
+      k = e;
+      continue;
+    }
+    // windows k .. e-1: one run
+    if (!args) args = std::make_unique<VideoArgs>();
+    VideoArgs* A = args.get();
+    std::memset(A, 0, sizeof(VideoArgs));
+    std::vector<const uint8_t*> w0(static_cast<size_t>(L));
+    for (int i = 0; i < L; ++i) w0[static_cast<size_t>(i)] = frames[win_indices[win_start[k] + i]];
+    cp_stack s0;
+    std::memset(&s0, 0, sizeof s0);
+    s0.n = L;
+    s0.width = width;
+    s0.height = height;
+    s0.channels = channels;
+    s0.frames = w0.data();
+    int rc = prepare_stack(ctx, &s0, params, w0.data(), &A->S);
+    if (rc) return rc;
+    if (!A->S.fast_int) return CP_OK;
+    const int smem = video_smem_bytes(L);
+    if (smem > ctx->max_smem) return CP_OK;
+    int per_sm = 1;
+    {
+      const auto key = std::make_pair(3000 + og * 16 + bg_first * 8 + A->S.nw, smem);
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      auto it = ctx->occupancy.find(key);
+      if (it != ctx->occupancy.end()) {
+        per_sm = it->second;
+      } else {
+        per_sm = video_slide(A, og, bg_first, true, 0, smem, nullptr, nullptr);
+        if (per_sm < 1) per_sm = 1;
+        ctx->occupancy[key] = per_sm;
+      }
+    }
+    A->npx = width * height;
+    A->tiles = (A->npx + 31) / 32;
+    const int grid = std::max(1, std::min(A->tiles, per_sm * ctx->sm_count));
+    const int per_launch = std::min(kVideoMaxWin, kVideoMaxRows - L + 1);
+    for (int k0 = k; k0 < e; k0 += per_launch) {
+      const int nw = std::min(per_launch, e - k0);
+      A->n_win = nw;
+      A->n_rows = nw + L - 1;
+      // row j of the launch: frame j of window k0 for j < L, then the last frame of window
+      // k0 + j - L + 1
+      for (int j = 0; j < A->n_rows; ++j) {
+        const int idx = j < L ? win_indices[win_start[k0] + j]
+                              : win_indices[win_start[k0 + j - L + 1] + L - 1];
+        A->rows[j] = frames[idx];
+      }
+      for (int w = 0; w < nw; ++w) {
+        A->outs[w] = outs[k0 + w];
+        A->blends[w] = out_blends ? out_blends[k0 + w] : nullptr;
+        if (!A->outs[w]) return CP_ERR_ARG;
+      }
+      A->warnings = warnings ? reinterpret_cast<unsigned long long*>(warnings + k0) : nullptr;
+      rc = video_slide(A, og, bg_first, false, grid, smem, st, ctx->d_error);
+      if (rc) return cuda_status(ctx, static_cast<cudaError_t>(rc), "sliding-window launch");
+    }
+    for (int w = k; w < e; ++w) done[static_cast<size_t>(w)] = 1;
+    k = e;
+  }
+  (void)image_count;
+  return CP_OK;
+}
+
 extern "C" int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* frames,
                                          int32_t image_count, int32_t width, int32_t height,
                                          int32_t channels, int32_t n_windows,
@@ -271,6 +386,21 @@ extern "C" int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* fram
   if (!ctx || !frames || !win_start || !win_len || !win_indices || !params || !outs ||
       n_windows < 0 || image_count < 1)
     return CP_ERR_ARG;
+  for (int k = 0; k < n_windows; ++k)
+    for (int i = 0; i < win_len[k]; ++i) {
+      const int idx = win_indices[win_start[k] + i];
+      if (idx < 0 || idx >= image_count || !frames[idx]) return CP_ERR_ARG;
+    }
+  std::vector<char> done(static_cast<size_t>(n_windows), 0);
+  // CP_VIDEO_SLIDING=0 in the environment sends every window to the batched kernel (for
+  // comparing the two paths on one workload)
+  const char* sliding_env = std::getenv("CP_VIDEO_SLIDING");
+  if (!sliding_env || std::strcmp(sliding_env, "0") != 0) {
+    const int rc = video_sliding(ctx, frames, image_count, width, height, channels, n_windows,
+                                 win_start, win_len, win_indices, params, outs, out_blends,
+                                 warnings, stream, done);
+    if (rc) return rc;
+  }
   std::vector<cp_stack> stacks;
   std::vector<cp_params> ps;
   std::vector<uint8_t*> o, b;
@@ -279,7 +409,7 @@ extern "C" int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* fram
   tables.reserve(static_cast<size_t>(n_windows));
   for (int k = 0; k < n_windows; ++k) {
     const int len = win_len[k];
-    if (len <= 0) continue;
+    if (len <= 0 || done[static_cast<size_t>(k)]) continue;
     std::vector<const uint8_t*> t(static_cast<size_t>(len));
     for (int i = 0; i < len; ++i) {
       const int idx = win_indices[win_start[k] + i];

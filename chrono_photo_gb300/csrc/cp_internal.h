@@ -166,6 +166,28 @@ inline int single_variant(const StackDev& s) {
   return 1 + k * 8 + g * 2 + b;
 }
 
+// Chrono-video windows sliding by one frame (cp_video.cu): the kernel's parameter block.
+// Window k of a launch reads frame rows k .. k + n - 1; longer calls are split into
+// launches of at most kVideoMaxWin windows.
+constexpr int kVideoMaxRows = 768;
+constexpr int kVideoMaxWin = 640;
+struct VideoArgs {
+  StackDev S;      // options of every window (S.n = window length); frame tables unused
+  int32_t n_rows;  // frame rows of this launch
+  int32_t n_win;   // windows of this launch
+  int32_t npx;     // pixels per frame
+  int32_t tiles;   // 32-pixel tiles per frame
+  const uint8_t* rows[kVideoMaxRows];
+  uint8_t* outs[kVideoMaxWin];
+  uint8_t* blends[kVideoMaxWin];  // entries may be null
+  unsigned long long* warnings;   // nullable: one counter per window of this launch
+};
+int video_smem_bytes(int n);
+// og: outlier group (1 extreme/first/last, 2 average, 3 forward/backward); bg_first: the
+// background is `first`. occupancy_only: returns CTAs per SM instead of launching.
+int video_slide(const void* args, int og, int bg_first, bool occupancy_only, int grid, int smem,
+                void* stream, uint32_t* error);
+
 // Shake search (cp_shake.cu): diffs[(f-1) * S^2 + oy*S + ox] for frames 1..n-1.
 int launch_shake(const uint8_t* const* frames_dev, int32_t n, int32_t width, int32_t height,
                  int32_t channels, const int32_t* anchors_dev, int32_t n_anchors, int32_t r,

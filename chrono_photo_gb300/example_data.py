@@ -230,3 +230,45 @@ def shake_stack_device(n, w, h, max_shift, seed):
         out[i] = torch.clamp(torch.floor(f + 0.5), 0, 255).to(torch.uint8)
     torch.cuda.synchronize()
     return out, shifts
+
+
+def stack_device(n, w, h, sigma=3.0, n_disks=1, rmin=20, rmax=20, seed=1, path="line",
+                 drift=0.0):
+    """The `stack` recipe generated on the CUDA device with torch, for benchmark workloads too
+    large for the host generator (300 frames of 1080p take about a minute in numpy): the same
+    gradient background, per-frame gain, Gaussian noise and disks with the same seeded
+    geometry, but the noise comes from torch's generator, so the frames are not the host
+    generator's. Returns a uint8 [n, h, w, 3] device tensor whose storage has 16 spare bytes
+    after the last frame (the kernels' 16-byte row copies may read up to there)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    dev = torch.device("cuda")
+    base = torch.from_numpy(_background(rng, w, h)).to(dev)
+    disks = [Disk(rng, w, h, n, rmin, rmax, path) for _ in range(n_disks)]
+    gains = rng.uniform(1 - drift, 1 + drift, size=n) if drift else np.ones(n)
+    flat = torch.zeros(n * h * w * 3 + 16, dtype=torch.uint8, device=dev)
+    out = flat[:n * h * w * 3].view(n, h, w, 3)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    for i in range(n):
+        f = base * float(gains[i]) + float(sigma) * torch.randn((h, w, 3), generator=gen,
+                                                                device=dev)
+        for dsk in disks:
+            cx, cy = dsk.center(i)
+            x0, x1 = max(int(cx - dsk.r) - 1, 0), min(int(cx + dsk.r) + 2, w)
+            y0, y1 = max(int(cy - dsk.r) - 1, 0), min(int(cy + dsk.r) + 2, h)
+            if x0 >= x1 or y0 >= y1:
+                continue
+            yy = torch.arange(y0, y1, device=dev, dtype=torch.float32)[:, None]
+            xx = torch.arange(x0, x1, device=dev, dtype=torch.float32)[None, :]
+            m = (xx - float(cx)) ** 2 + (yy - float(cy)) ** 2 <= dsk.r ** 2
+            f[y0:y1, x0:x1][m] = torch.tensor([float(v) for v in dsk.color], device=dev)
+        out[i] = torch.clamp(torch.floor(f + 0.5), 0, 255).to(torch.uint8)
+    torch.cuda.synchronize()
+    return out
+
+
+def video_stack_device(seed=3, n=300, w=1920, h=1080):
+    """video_stack's recipe on the device (see stack_device)."""
+    return stack_device(n, w, h, sigma=4, n_disks=1, rmin=30, rmax=30, seed=seed, path="sine",
+                        drift=0.05)
