@@ -89,6 +89,7 @@ SIGNATURES = [
     ("cp_ctx_last_error", ct.c_int, [P, ct.c_char_p, ct.c_size_t]),
     ("cp_ctx_stream", P, [P]),
     ("cp_ctx_synchronize", ct.c_int, [P]),
+    ("cp_ctx_set_wait_limit", ct.c_int, [P, U64]),
     ("cp_dev_alloc", ct.c_int, [P, U64, ct.POINTER(P)]),
     ("cp_dev_free", ct.c_int, [P, P]),
     ("cp_host_alloc", ct.c_int, [P, U64, ct.POINTER(P)]),

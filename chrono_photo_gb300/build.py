@@ -32,9 +32,13 @@ KERNEL_VARIANTS = [(3, k, g, b) for k in (1, 2) for b in (1, 0) for g in (1, 2, 
      (4, 3, 0, 0)]
 # cp_kernels_batch_variant.cu: the CP_BATCH_VARIANTS list of cp_internal.h
 BATCH_VARIANTS = [(3, k, g, 1) for k in (1, 2) for g in (1, 2, 3)]
+# cp_kernels_px.cu compiled once per pixel-thread kernel family (distance kind, outlier
+# group, background): the CP_PX_VARIANTS list of cp_internal.h
+PX_VARIANTS = [(k, g, b) for k in (1, 2) for b in (1, 0) for g in (1, 2, 3)]
 CPP_SOURCES = ["cp_host.cpp", "cp_stage.cpp", "cp_batch.cpp", "cp_shake_host.cpp",
                "cp_server.cpp", "cp_ingest.cpp", "cp_png_write.cpp"]
-HEADERS = ["cp_internal.h", "cp_host_internal.h", "cp_tile.cuh", "cp_png.h"]
+HEADERS = ["cp_internal.h", "cp_host_internal.h", "cp_tile.cuh", "cp_png.h", "cp_pixel.cuh",
+           "cp_outlier_px.cuh"]
 
 
 def _cuda_home():
@@ -109,6 +113,14 @@ def build(verbose=False, jobs=None):
             steps.append([nvcc] + ARCH + NVCC_FLAGS + [
                 "-DCP_CH=%d" % ch, "-DCP_KIND=%d" % kind, "-DCP_OG=%d" % og, "-DCP_BG=%d" % bg,
                 "-c", bsrc, "-o", o])
+    psrc = os.path.join(CSRC, "cp_kernels_px.cu")
+    for kind, og, bg in PX_VARIANTS:
+        o = os.path.join(OBJ_DIR, "cp_kernels_px_k%d_g%d_b%d.o" % (kind, og, bg))
+        objs.append(o)
+        if _stale(o, [psrc] + hdrs):
+            steps.append([nvcc] + ARCH + NVCC_FLAGS + [
+                "-DCP_KIND=%d" % kind, "-DCP_OG=%d" % og, "-DCP_BG=%d" % bg,
+                "-c", psrc, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ_DIR, src + ".o")

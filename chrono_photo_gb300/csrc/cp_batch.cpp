@@ -266,7 +266,7 @@ extern "C" int cp_composite_batch_device(cp_ctx* ctx, const cp_stack* stacks,
 // step 1: every window of the steady middle part of create_video, src/main.rs:230-286) run
 // the sliding kernel (cp_video.cu) when the options allow it: RGB, outlier mode with an abs
 // threshold and 0/1 weights (integer distances), no fade, no --sample, 16-byte aligned
-// frames. Each maximal run of at least kMinSlideRun windows of one length 2..CP_MAX_FRAMES,
+// frames. Each maximal run of at least kMinSlideRun windows of one length 2..64,
 // each window the previous one shifted by one frame, is one run; done[k] marks the windows
 // handled here, the rest (the growing and shrinking windows at the ends) go to the batched
 // kernel.
@@ -302,7 +302,7 @@ static int video_sliding(cp_ctx* ctx, const uint8_t* const* frames, int32_t imag
   int k = 0;
   while (k < n_windows) {
     const int L = win_len[k];
-    if (L < 2 || L > CP_MAX_FRAMES || !aligned(k)) {
+    if (L < 2 || L > 64 || !aligned(k)) {
       ++k;
       continue;
     }

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -252,6 +253,7 @@ int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
     quantile_spec(len, 0.75f, &d->q3_k, &d->q3_pair, &d->q3_frac);
   }
   d->seed = p->rng_seed;
+  d->wait_cycles = (ctx && ctx->wait_cycles > 0) ? ctx->wait_cycles : kDefaultWaitCycles;
   if (fade_lut(&p->fade, n, st->frame_offset, d->fade) != CP_OK) {
     ctx_error(ctx, "invalid fade specification");
     return CP_ERR_ARG;
@@ -293,6 +295,47 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
       default: rc = launch_simple_stream_c4(d, fast, grid, stream, ctx->d_error); break;
     }
     return cuda_status(ctx, static_cast<cudaError_t>(rc), "simple launch");
+  }
+  if (d.mode == CP_MODE_OUTLIER && d.channels == 3 && !d.shifted && !d.has_crop &&
+      (d.fast_int || d.pair_f32)) {
+    // the pixel-thread kernel (cp_outlier_px.cuh), single-buffered staging (measured faster
+    // than double buffering, which costs a resident CTA per SM); CP_PX_BUFFERS=2 selects
+    // double buffering up to 64 frames
+    int k, g, b;
+    outlier_variant(d, &k, &g, &b);
+    const char* nb = std::getenv("CP_PX_BUFFERS");
+    const bool db = d.nw <= 2 && nb && std::strcmp(nb, "2") == 0;
+    const int psmem = px_smem_bytes(d.n, db);
+    if (psmem <= ctx->max_smem) {
+      const auto key = std::make_pair(4000 + 64 * k + 8 * g + 2 * b + (db ? 1 : 0), psmem);
+      int per_sm = 0, rc = -1;
+      {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        auto it = ctx->occupancy.find(key);
+        if (it != ctx->occupancy.end()) per_sm = it->second;
+      }
+      if (per_sm == 0) {
+#define CP_PX_OCC(K, G, B)                                                               \
+  if (k == K && g == G && b == B)                                                        \
+    per_sm = px_launch_k##K##_g##G##_b##B(d, db, true, 0, psmem, nullptr, nullptr);
+        CP_PX_VARIANTS(CP_PX_OCC)
+#undef CP_PX_OCC
+        if (per_sm < 1) per_sm = 1;
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        ctx->occupancy[key] = per_sm;
+      }
+      const int grid = std::max(1, std::min(d.tiles, per_sm * ctx->sm_count));
+#define CP_PX_RUN(K, G, B)                                                               \
+  if (k == K && g == G && b == B)                                                        \
+    rc = px_launch_k##K##_g##G##_b##B(d, db, false, grid, psmem, stream, ctx->d_error);
+      CP_PX_VARIANTS(CP_PX_RUN)
+#undef CP_PX_RUN
+      if (rc < 0) {
+        ctx_error(ctx, "no pixel-thread kernel for variant %d/%d/%d", k, g, b);
+        return CP_ERR_ARG;
+      }
+      return cuda_status(ctx, static_cast<cudaError_t>(rc), "composite launch");
+    }
   }
   const int smem = smem_bytes_for(d.n, d.channels);
   if (smem > ctx->max_smem) {
@@ -656,6 +699,12 @@ int cp_ctx_synchronize(cp_ctx* ctx) {
   int rc = cuda_status(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
   if (rc) return rc;
   return check_device_error(ctx);
+}
+
+int cp_ctx_set_wait_limit(cp_ctx* ctx, uint64_t cycles) {
+  if (!ctx || cycles > (uint64_t(1) << 62)) return CP_ERR_ARG;
+  ctx->wait_cycles = static_cast<int64_t>(cycles);
+  return CP_OK;
 }
 
 int cp_dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr) {

@@ -54,6 +54,7 @@ struct cp_ctx {
   std::map<void*, uint64_t> allocs;
   std::map<std::pair<int, int>, int> occupancy;  // (kernel key, smem) -> CTAs per SM
   uint32_t* d_error = nullptr;               // device error flags of bounded waits
+  int64_t wait_cycles = 0;                   // bounded-wait limit of launches (0: default)
   unsigned long long* d_warn = nullptr;      // device warning counter (host-staged calls)
   // host-staged composite: device copies of the frames and outputs, pinned staging
   cp::DevBuffer frames_dev, out_dev, blend_dev, dbg_dev;

@@ -7,6 +7,7 @@
 namespace cp {
 
 constexpr int kTilePx = 128;      // pixels per tile: 32 columns, served by `channels` warps
+constexpr long long kDefaultWaitCycles = 1ll << 32;  // ~2 s: the default bounded-wait limit
 inline int cta_threads(int channels) { return 32 * channels; }
 
 // Shared-memory exchange area of a compositing tile, behind its staged frame rows: warp w
@@ -86,6 +87,8 @@ struct StackDev {
   float q3_frac;
   uint32_t sample_mask[4];  // frames in the (sub)sample, bit i of word i/32
   uint64_t seed;
+  int64_t wait_cycles;  // SM clock cycles before a bounded wait gives up
+  uint64_t pad0;        // keeps the descriptor a multiple of 16 bytes (copied in 16-byte words)
   // per-frame tables
   const uint8_t* frames[CP_MAX_FRAMES];
   int32_t crop[2 * CP_MAX_FRAMES];
@@ -166,13 +169,37 @@ inline int single_variant(const StackDev& s) {
   return 1 + k * 8 + g * 2 + b;
 }
 
+// Pixel-thread single-stack outlier kernel (cp_outlier_px.cuh): RGB stacks with 16-byte
+// aligned frame rows and no crop, distance kind 1 (integer) or 2 (paired f32). A CTA of
+// kPxThreads threads; phase A's order statistics reach the pixel threads through PxAux.
+constexpr int kPxThreads = 128;
+struct PxAux {
+  uint32_t lo[4][32], hi[4][32];  // word w of column t; word 3 is zero (funnel padding)
+  float wq[12][32];               // rel: w * iqr_inv of byte position q of column t
+  uint32_t out[3][32], blend[3][32];
+};
+// header + one or two (double-buffered) stage buffers of n rows + PxAux
+inline int px_smem_bytes(int n, bool db) {
+  return kSmemHeader + (db ? 2 : 1) * n * row_pitch_host(3) + static_cast<int>(sizeof(PxAux));
+}
+// (distance kind, outlier group, background) of the compiled pixel-thread kernels; each
+// translation unit holds plane-word counts 1, 2 (single and double buffered) and 4 (single).
+#define CP_PX_VARIANTS(X)                                                                    \
+  X(1, 1, 1) X(1, 2, 1) X(1, 3, 1) X(1, 1, 0) X(1, 2, 0) X(1, 3, 0) X(2, 1, 1) X(2, 2, 1)  \
+  X(2, 3, 1) X(2, 1, 0) X(2, 2, 0) X(2, 3, 0)
+#define CP_DECLARE_PX(K, G, B)                                                               \
+  int px_launch_k##K##_g##G##_b##B(const StackDev& s, bool db, bool occupancy_only, int grid, \
+                                   int smem, void* stream, uint32_t* error);
+CP_PX_VARIANTS(CP_DECLARE_PX)
+#undef CP_DECLARE_PX
+
 // Chrono-video windows sliding by one frame (cp_video.cu): the kernel's parameter block.
 // Window k of a launch reads frame rows k .. k + n - 1; longer calls are split into
 // launches of at most kVideoMaxWin windows.
 constexpr int kVideoMaxRows = 768;
 constexpr int kVideoMaxWin = 640;
 struct VideoArgs {
-  StackDev S;      // options of every window (S.n = window length); frame tables unused
+  StackDev S;      // options of every window (S.n = window length <= 64); frame tables unused
   int32_t n_rows;  // frame rows of this launch
   int32_t n_win;   // windows of this launch
   int32_t npx;     // pixels per frame

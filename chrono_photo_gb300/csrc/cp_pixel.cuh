@@ -1,0 +1,405 @@
+// cp_pixel.cuh — the per-pixel half of outlier compositing with one thread per pixel: the
+// pixel's statistics from its channels' order statistics, the distance pass over its samples
+// (src/chrono.rs:257-288) and the epilogue (background, outlier pick and blend, blend mask,
+// src/chrono.rs:290-493). Shared by the pixel-thread single-stack kernel (cp_outlier_px.cuh)
+// and the sliding-window kernel (cp_video.cu). `load(i)` returns sample i of the pixel as a
+// word with its channel bytes in bytes 0..C-1; the bytes above may hold anything (the
+// distance arithmetic masks them, the epilogue masks its loads).
+//
+// The arithmetic is the tile kernel's (cp_tile.cuh), in the reference's f32 operation order
+// with explicit _rn intrinsics.
+
+#pragma once
+#include "cp_tile.cuh"
+
+namespace cp {
+namespace {
+
+template <int C>
+struct PxStat {
+  uint32_t klo, khi;  // floor / ceil of the medians, channel bytes (integer distances)
+  int nh;             // channels with a half-integer median
+  float med[C];       // median() per channel, 0 for weight-0 channels (src/chrono.rs:238-255)
+  float medo[C];      // med + 2^22 (exact)
+  float wi[C];        // w * iqr_inv (rel thresholds) or w (abs)
+};
+
+// lo3 / hi3: d[k] and d[k+1] (or d[k] again without a pair) of the median per channel byte;
+// wq: w * iqr_inv per channel for rel thresholds (ignored for abs).
+template <int C>
+DEVI PxStat<C> px_stat(const StackDev& S, uint32_t lo3, uint32_t hi3, const float (&wq)[C]) {
+  PxStat<C> r;
+  r.klo = r.khi = 0u;
+  r.nh = 0;
+#pragma unroll
+  for (int ch = 0; ch < C; ++ch) {
+    const uint32_t lo = (lo3 >> (8 * ch)) & 0xFFu, hi = (hi3 >> (8 * ch)) & 0xFFu;
+    const bool wt = (S.wmask >> ch) & 1u;
+    r.med[ch] = !wt ? 0.0f
+                    : (S.med_pair ? __fmul_rn(0.5f, __fadd_rn(static_cast<float>(lo),
+                                                              static_cast<float>(hi)))
+                                  : static_cast<float>(lo));
+    r.medo[ch] = __fadd_rn(r.med[ch], 4194304.0f);
+    r.wi[ch] = S.thr_abs ? S.w[ch] : wq[ch];
+    const uint32_t s2 = lo + hi;
+    const uint32_t fl = S.med_pair ? (s2 >> 1) : lo, ce = S.med_pair ? ((s2 + 1) >> 1) : lo;
+    if (wt) {
+      r.klo |= fl << (8 * ch);
+      r.khi |= ce << (8 * ch);
+      r.nh += static_cast<int>(ce - fl);
+    }
+  }
+  return r;
+}
+
+// Largest-distance bookkeeping is compiled in for the outlier groups that pick `extreme`.
+template <int OG>
+constexpr bool kKeepMax = OG == kOgAny || OG == kOgSingle;
+
+// Distance pass over samples 0..n-1 (src/chrono.rs:257-288): outlier flags pb (bit i of word
+// i/32), and for `extreme` the largest distance, earliest sample first: integer kind as the
+// key (D' << 8) + 255 - i (key < 0: none), f32 kinds as (dmax, imax).
+template <int C, int NW, int KIND, int OG, typename Load>
+DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wbytes, Load load,
+                      uint32_t (&pb)[NW], int32_t& key, float& dmax, int& imax) {
+  key = st.nh > 0 ? -1 : 255;
+  dmax = 0.0f;
+  imax = 0;
+  if (KIND == kIntKind || (KIND == kAnyKind && S.fast_int)) {
+    const int32_t thr1 = S.thr_int[st.nh] - 1;
+#pragma unroll
+    for (int blk = 0; blk < NW; ++blk) {
+      // flags enter at bit 0 and move up (a funnel shift takes the sign of thr - 1 - d:
+      // set iff d >= thr); one bit reversal puts sample i at bit i
+      uint32_t ob = 0u;
+      const int i0 = blk * 32, iend = min(n, i0 + 32);
+#pragma unroll 4
+      for (int i = i0; i < iend; ++i) {
+        const int32_t d = static_cast<int32_t>(dist_int(load(i), wbytes, st.klo, st.khi));
+        ob = __funnelshift_l(static_cast<uint32_t>(thr1 - d), ob, 1);
+        if (kKeepMax<OG>) {
+          const int32_t kv = (d << 8) + 255 - i;
+          key = kv > key ? kv : key;
+        }
+      }
+      pb[blk] = iend > i0 ? __brev(ob) >> (32 - (iend - i0)) : 0u;
+    }
+  } else if (KIND == kF32Kind || (KIND == kAnyKind && S.pair_f32)) {
+    // two samples per instruction in float2 lanes, every term on (median - p) / 2: the
+    // sample -(2^14 + p/2) is one byte permute of the pixel byte into -2^14's mantissa, the
+    // median 2^14 + median/2 is exact, so terms, sums and the threshold are the reference's
+    // values times exactly 1/4 (ranges checked on the host). Products are summed with scalar
+    // adds: a paired add after a paired multiply was contracted into a fused multiply-add.
+    float2 mq[C], wq2[C];
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) {
+      const float m = __fadd_rn(__fmul_rn(__fsub_rn(st.medo[ch], 4194304.0f), 0.5f), 16384.0f);
+      mq[ch] = make_float2(m, m);
+      wq2[ch] = make_float2(st.wi[ch], st.wi[ch]);
+    }
+    const float thr4 = __fmul_rn(S.thr_sq, 0.25f);
+#pragma unroll
+    for (int blk = 0; blk < NW; ++blk) {
+      uint32_t ob = 0u;
+      const int iend = min(n, blk * 32 + 32);
+      for (int i = blk * 32; i < iend; i += 2) {
+        const uint32_t p0 = load(i);
+        const uint32_t p1 = i + 1 < iend ? load(i + 1) : p0;
+        float2 dq = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+          if (!((S.wmask >> ch) & 1u)) continue;
+          const uint32_t sel = 0x7604u | (static_cast<uint32_t>(ch) << 4);
+          const float2 nv = make_float2(__uint_as_float(__byte_perm(p0, 0xC6800000u, sel)),
+                                        __uint_as_float(__byte_perm(p1, 0xC6800000u, sel)));
+          const float2 tt = mul2_rn(wq2[ch], add2_rn(mq[ch], nv));
+          const float2 sq = mul2_rn(tt, tt);
+          dq.x = __fadd_rn(dq.x, sq.x);
+          dq.y = __fadd_rn(dq.y, sq.y);
+        }
+        const bool o0 = dq.x >= thr4;
+        ob |= o0 ? (1u << (i & 31)) : 0u;
+        if (kKeepMax<OG>) {
+          const bool up = o0 && dq.x > dmax;
+          dmax = up ? dq.x : dmax;
+          imax = up ? i : imax;
+        }
+        if (i + 1 < iend) {
+          const bool o1 = dq.y >= thr4;
+          ob |= o1 ? (1u << ((i + 1) & 31)) : 0u;
+          if (kKeepMax<OG>) {
+            const bool up = o1 && dq.y > dmax;
+            dmax = up ? dq.y : dmax;
+            imax = up ? i + 1 : imax;
+          }
+        }
+      }
+      pb[blk] = ob;
+    }
+    dmax = __fmul_rn(dmax, 4.0f);  // scaled back exactly
+  } else {
+#pragma unroll
+    for (int blk = 0; blk < NW; ++blk) {
+      uint32_t ob = 0u;
+      const int iend = min(n, blk * 32 + 32);
+      for (int i = blk * 32; i < iend; ++i) {
+        const uint32_t px = load(i);
+        const float d = S.finite_w ? dist_f32<C, true>(S, st.medo, st.wi, px)
+                                   : dist_f32<C, false>(S, st.medo, st.wi, px);
+        const bool o = d >= S.thr_sq;
+        ob |= o ? (1u << (i & 31)) : 0u;
+        if (kKeepMax<OG>) {
+          const bool up = o && d > dmax;
+          dmax = up ? d : dmax;
+          imax = up ? i : imax;
+        }
+      }
+      pb[blk] = ob;
+    }
+  }
+}
+
+struct PxOut {
+  uint32_t pix;   // composite, channel bytes
+  uint32_t mask;  // blend mask value of channels 0..2
+  int chosen;     // debug: sample blended in (-1 none, -2 several), or 0 for an averaged pick
+  int bg_idx;     // debug: background sample (first / random), else -1
+  int nout;
+  bool warning;   // every sample an outlier under a first / random background
+};
+
+// The epilogue of one pixel (src/chrono.rs:290-493). sums: the channel sums over all n
+// samples for the average background (computed here when null).
+template <int C, int NW, int KIND, int OG, int BG, typename Load>
+DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t wbytes,
+                       const uint32_t (&pb)[NW], int32_t key, float dmax_f, int imax_f,
+                       int pix_idx, const uint32_t* sums, Load load_raw) {
+  PxOut r;
+  auto load = [&](int i) -> uint32_t { return load_raw(i) & (0xFFFFFFFFu >> (32 - 8 * C)); };
+  const bool fast = KIND == kIntKind || (KIND == kAnyKind && S.fast_int);
+  auto dsq_px = [&](uint32_t px) -> float {  // dist_sq of a sample, recomputed
+    if (fast)
+      return static_cast<float>(dist_int(px, wbytes, st.klo, st.khi)) +
+             0.25f * static_cast<float>(st.nh);
+    if constexpr (KIND == kF32Kind) return dist_f32<C, true, false>(S, st.medo, st.wi, px);
+    return S.finite_w ? dist_f32<C, true>(S, st.medo, st.wi, px)
+                      : dist_f32<C, false>(S, st.medo, st.wi, px);
+  };
+  int nout = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) nout += __popc(pb[w]);
+  const int bgm = BG == kBgFirst ? CP_BG_FIRST : S.background;
+  bool warning = false;
+  int bg_idx = -1;
+  uint32_t pix = 0;
+  // background, src/chrono.rs:293-375
+  if (bgm == CP_BG_FIRST || bgm == CP_BG_RANDOM) {
+    if (bgm == CP_BG_FIRST) {
+      if (nout == 0) {
+        bg_idx = 0;
+      } else if (nout == n) {
+        bg_idx = 0;
+        warning = true;
+      } else {
+        uint32_t inv[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) inv[w] = ~pb[w];
+        bg_idx = first_set<NW>(inv);  // first_excluded, src/chrono.rs:504-530
+      }
+    } else {
+      const uint64_t pid = static_cast<uint64_t>(pix_idx);
+      if (nout == 0 || nout == n) {
+        bg_idx = static_cast<int>(gen_range(S.seed, pid, static_cast<uint32_t>(n)));
+        warning = nout == n;
+      } else {
+        // sample_excluded, src/chrono.rs:531-555: the j-th outlier (ascending) was swapped
+        // with position n-1-j; trace the drawn position back through the swaps.
+        int pos = static_cast<int>(gen_range(S.seed, pid, static_cast<uint32_t>(n - nout)));
+        int j = nout - 1;
+#pragma unroll
+        for (int w = NW - 1; w >= 0; --w) {
+          uint32_t m = pb[w];
+          while (m) {
+            const int bpos = 31 - __clz(m);
+            m &= ~(1u << bpos);
+            const int a = 32 * w + bpos, b = n - 1 - j;
+            if (pos == a)
+              pos = b;
+            else if (pos == b)
+              pos = a;
+            --j;
+          }
+        }
+        bg_idx = pos;
+      }
+    }
+    pix = load(bg_idx);
+  } else if (bgm == CP_BG_AVERAGE) {
+    uint32_t sum[C];
+    if (sums) {
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) sum[ch] = sums[ch];
+    } else {
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) sum[ch] = 0u;
+      for (int i = 0; i < n; ++i) {
+        const uint32_t px = load(i);
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) sum[ch] += (px >> (8 * ch)) & 0xFFu;
+      }
+    }
+    const float nf = static_cast<float>(n);
+    if (nout == 0) {
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch)
+        pix |= sat_u8(rround(__fdiv_rn(static_cast<float>(sum[ch]), nf))) << (8 * ch);
+    } else {
+      uint32_t osum[C];
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) osum[ch] = 0u;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        uint32_t m = pb[w];
+        while (m) {
+          const int bpos = __ffs(m) - 1;
+          m &= m - 1;
+          const uint32_t px = load(32 * w + bpos);
+#pragma unroll
+          for (int ch = 0; ch < C; ++ch) osum[ch] += (px >> (8 * ch)) & 0xFFu;
+        }
+      }
+      // src/chrono.rs:307-333 (the reference's own formula, incl. k = n -> inf)
+      const float ratio = __fdiv_rn(nf, static_cast<float>(n - nout));
+#pragma unroll
+      for (int ch = 0; ch < C; ++ch) {
+        const float mean = __fdiv_rn(static_cast<float>(sum[ch]), nf);
+        const float v = __fsub_rn(__fmul_rn(mean, ratio),
+                                  __fdiv_rn(static_cast<float>(osum[ch]), nf));
+        pix |= sat_u8(rround(v)) << (8 * ch);
+      }
+    }
+  } else {  // median (outliers included), src/chrono.rs:340-345
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(st.med[ch])) << (8 * ch);
+  }
+
+  // outlier pick and blend, src/chrono.rs:377-493
+  float blend = 0.0f;
+  int chosen = -1;
+  uint32_t mask = 0;
+  const bool single_group = og_is<OG>(S, kOgSingle);
+  const bool blend_group = og_is<OG>(S, kOgBlend);
+  const bool extreme = single_group && S.outlier == CP_OUTLIER_EXTREME;
+  const bool multi = nout > 1 && !single_group;
+  if (!multi) {
+    int si;
+    float dsq = 0.0f;
+    if (extreme) {
+      if (fast) {
+        si = key < 0 ? 0 : 255 - (key & 255);
+        const int32_t dm = key < 0 ? -1 : (key >> 8);
+        dsq = dm < 0 ? 0.0f : static_cast<float>(dm) + 0.25f * static_cast<float>(st.nh);
+      } else {
+        si = imax_f;
+        dsq = dmax_f;
+      }
+    } else {
+      // the multi-outlier groups come here with at most one outlier: first == last
+      si = (single_group && S.outlier == CP_OUTLIER_LAST) ? last_set<NW>(pb) : first_set<NW>(pb);
+      si = si < 0 ? 0 : si;
+    }
+    const uint32_t sample = load(si);
+    if (!extreme) dsq = dsq_px(sample);
+    blend = nout == 0 ? 0.0f : __fmul_rn(S.fade[si], blend_value(S, __fsqrt_rn(dsq)));
+    pix = blend_into_u8<C>(pix, sample, blend);
+    mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
+    chosen = nout == 0 ? -1 : si;
+  } else if (blend_group) {
+    float pf[C];
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((pix >> (8 * ch)) & 0xFFu);
+    float binv = 1.0f;
+    auto blend_one = [&](int f) {
+      const uint32_t sv = load(f);
+      const float bk = __fmul_rn(S.fade[f], blend_value(S, __fsqrt_rn(dsq_px(sv))));
+      // blend_into_f32_u8, src/color.rs:32-44
+      if (bk <= 0.0f) {
+      } else if (bk >= 1.0f) {
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) pf[ch] = static_cast<float>((sv >> (8 * ch)) & 0xFFu);
+      } else {
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+          const float x = static_cast<float>((sv >> (8 * ch)) & 0xFFu);
+          pf[ch] = __fadd_rn(pf[ch], __fmul_rn(__fsub_rn(x, pf[ch]), bk));
+        }
+      }
+      binv = __fmul_rn(binv, __fsub_rn(1.0f, bk));
+    };
+    // outliers in ascending (forward) or descending (backward) sample order
+    if (S.outlier == CP_OUTLIER_FORWARD) {
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        uint32_t m = pb[w];
+        while (m) {
+          const int f = 32 * w + __ffs(m) - 1;
+          m &= m - 1;
+          blend_one(f);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int w = NW - 1; w >= 0; --w) {
+        uint32_t m = pb[w];
+        while (m) {
+          const int bpos = 31 - __clz(m);
+          m &= ~(1u << bpos);
+          blend_one(32 * w + bpos);
+        }
+      }
+    }
+    pix = 0;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(pf[ch])) << (8 * ch);
+    mask = sat_u8(rround(__fmul_rn(__fsub_rn(1.0f, binv), 255.0f)));
+    chosen = -2;
+  } else {  // average of several outliers, src/chrono.rs:429-468
+    // channel sums in 16-bit lanes (n * 255 < 2^16): even bytes, odd bytes
+    uint32_t se = 0u, so = 0u;
+    float mdist = 0.0f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      uint32_t m = pb[w];
+      while (m) {
+        const int f = 32 * w + __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t px = load(f);
+        se += px & 0x00FF00FFu;
+        so += (px >> 8) & 0x00FF00FFu;
+        mdist = __fadd_rn(mdist, __fsqrt_rn(dsq_px(px)));
+      }
+    }
+    const float kf = static_cast<float>(nout);
+    uint32_t sample = 0;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) {
+      const uint32_t os = ((ch & 1) ? so : se) >> (16 * (ch >> 1)) & 0xFFFFu;
+      sample |= sat_u8(rround(__fdiv_rn(static_cast<float>(os), kf))) << (8 * ch);
+    }
+    // the fade of an averaged outlier is taken at sample 0 (src/chrono.rs:467)
+    blend = __fmul_rn(S.fade[0], blend_value(S, __fdiv_rn(mdist, kf)));
+    pix = blend_into_u8<C>(pix, sample, blend);
+    mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
+    chosen = 0;
+  }
+  r.pix = pix;
+  r.mask = mask;
+  r.chosen = chosen;
+  r.bg_idx = bg_idx;
+  r.nout = nout;
+  r.warning = warning;
+  return r;
+}
+
+}  // namespace
+}  // namespace cp

@@ -37,7 +37,7 @@ namespace {
 
 #define DEVI __device__ __forceinline__
 
-constexpr long long kWaitCycles = 1ll << 32; // ~2 s at 2 GHz before a wait gives up
+constexpr long long kWaitCycles = kDefaultWaitCycles;  // ~2 s at 2 GHz before a wait gives up
 
 // ---- PTX wrappers ------------------------------------------------------------------------
 DEVI uint32_t smem_u32(const void* p) {
@@ -72,11 +72,13 @@ DEVI void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
-// Bounded wait on an mbarrier phase: false after ~2 s (the caller records an error).
-DEVI bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase: false once `limit` SM clock cycles have passed (the
+// caller records an error); a limit of 1 or less gives up without testing the phase.
+DEVI bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kWaitCycles) {
+  if (limit <= 1) return false;
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }
@@ -365,33 +367,34 @@ DEVI void build_planes(uint32_t (&P)[BP][8][NW], const Rows<C, SH>& rd, int w, i
 template <int NW, int BP>
 DEVI void select_rank(const uint32_t (&P)[BP][8][NW], const uint32_t (&S)[NW], int k,
                       uint32_t (&v)[BP]) {
+  // Per step: d = kk - (candidates with a 0 bit); its sign mask M (-1: rank kk lies among
+  // them) selects the half by one LOP3 per word (c & (P ^ M)) and keeps kk or d; the value
+  // bits accumulate as u = 2u + M (u = -(bits of the zero halves)), so v = 255 + u.
   uint32_t c[BP][NW];
-  int kk[BP];
+  int kk[BP], u[BP];
 #pragma unroll
   for (int j = 0; j < BP; ++j) {
 #pragma unroll
     for (int w = 0; w < NW; ++w) c[j][w] = S[w];
     kk[j] = k;
-    v[j] = 0u;
+    u[j] = 0;
   }
 #pragma unroll
   for (int b = 7; b >= 0; --b) {
 #pragma unroll
     for (int j = 0; j < BP; ++j) {
-      uint32_t z[NW];
-      int cz = 0;
+      int d = kk[j];
 #pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        z[w] = c[j][w] & ~P[j][b][w];
-        cz += __popc(z[w]);
-      }
-      const bool one = kk[j] >= cz;
+      for (int w = 0; w < NW; ++w) d -= __popc(c[j][w] & ~P[j][b][w]);
+      const int m = d >> 31;
 #pragma unroll
-      for (int w = 0; w < NW; ++w) c[j][w] = one ? (c[j][w] ^ z[w]) : z[w];  // c & P or c & ~P
-      kk[j] -= one ? cz : 0;
-      v[j] = (v[j] << 1) | static_cast<uint32_t>(one);
+      for (int w = 0; w < NW; ++w) c[j][w] &= P[j][b][w] ^ static_cast<uint32_t>(m);
+      kk[j] = (kk[j] & m) | (d & ~m);
+      u[j] = 2 * u[j] + m;
     }
   }
+#pragma unroll
+  for (int j = 0; j < BP; ++j) v[j] = static_cast<uint32_t>(255 + u[j]);
 }
 
 // quantile() of src/chrono.rs:567-579 from its order statistics: (1-frac)*d[p1] +
@@ -558,20 +561,18 @@ DEVI bool og_is(const StackDev& S, int og) {
   return m == CP_OUTLIER_EXTREME || m == CP_OUTLIER_FIRST || m == CP_OUTLIER_LAST;
 }
 
-template <int C, int NW, bool SH, int KIND, int OG, int BG>
-DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
-                       Aux<C, NW>& A, uint32_t& warn_count) {
+// (2)+(3) of a tile: bit planes of word wp of column t and the order statistics of its 4
+// byte positions: plo / phi = d[k], d[k+1] of the median per byte (d[k] twice without a pair),
+// and for rel thresholds wq[k] = w * iqr_inv (src/chrono.rs:220-255) and the debug quartiles.
+template <int C, int NW, bool SH, int KIND>
+DEVI void word_order_stats(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd, int wp,
+                           int t, uint32_t& plo_out, uint32_t& phi_out, float (&wq_out)[4]) {
   constexpr int BP = NW <= 2 ? 4 : 2;  // byte positions per plane build (register budget)
   const int n = S.n;
-  const int wp = static_cast<int>(threadIdx.x) >> 5;  // warp: word, frame class, pixels
-  const int t = static_cast<int>(threadIdx.x) & 31;   // column
   uint32_t smask[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
   const bool rel = KIND == kIntKind ? false : !S.thr_abs;  // the integer path is abs only
-
-  // (2)+(3) planes and order statistics of word wp, BP positions per round
-  {
     uint32_t plo = 0u, phi = 0u;
     float wq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -669,6 +670,24 @@ DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& r
         }
       }
     }
+    plo_out = plo;
+    phi_out = phi;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) wq_out[k] = wq[k];
+}
+
+template <int C, int NW, bool SH, int KIND, int OG, int BG>
+DEVI void outlier_tile(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd,
+                       Aux<C, NW>& A, uint32_t& warn_count) {
+  const int n = S.n;
+  const int wp = static_cast<int>(threadIdx.x) >> 5;  // warp: word, frame class, pixels
+  const int t = static_cast<int>(threadIdx.x) & 31;   // column
+
+  // (2)+(3) planes and order statistics of word wp, BP positions per round
+  {
+    uint32_t plo = 0u, phi = 0u;
+    float wq[4];
+    word_order_stats<C, NW, SH, KIND>(S, g, rd, wp, t, plo, phi, wq);
     A.lo[wp][t] = plo;
     A.hi[wp][t] = phi;
 #pragma unroll
@@ -1223,8 +1242,12 @@ DEVI bool run_tile(const StackDev& S, const TileGeo& g, const SmemLayout& L, uin
     issue_tile<C>(S, g, L.buf, L.shifts, L.fbase, L.bar);
   }
   __syncthreads();
-  if (!mbar_wait(L.bar, phase)) {
-    if (error) atomicOr(error, 1u);
+  // bounded wait; the CTA leaves together if any thread's wait gave up, once the copies in
+  // flight into its shared memory have landed
+  const bool ok = mbar_wait(L.bar, phase, S.wait_cycles);
+  if (__syncthreads_or(ok ? 0 : 1)) {
+    if (!ok) mbar_wait(L.bar, phase);
+    if (error && threadIdx.x == 0) atomicOr(error, 1u);
     return false;
   }
   phase ^= 1u;
@@ -1435,10 +1458,12 @@ __global__ void __launch_bounds__(kStreamThreads, 8)
         outw[p] = 0u;
       }
     }
-    if (!mbar_wait(&full[st], static_cast<uint32_t>(i / kStreamStages) & 1u)) {
-      if (error) atomicOr(error, 1u);
-      // the other stages' copies in flight complete (bounded) before the CTA leaves
-      for (int j = i + 1; j < min(i + kStreamStages, items); ++j)
+    const bool ok = mbar_wait(&full[st], static_cast<uint32_t>(i / kStreamStages) & 1u,
+                              S.wait_cycles);
+    if (__syncthreads_or(ok ? 0 : 1)) {
+      if (error && threadIdx.x == 0) atomicOr(error, 1u);
+      // every stage's copy in flight completes (bounded) before the CTA leaves
+      for (int j = i; j < min(i + kStreamStages, items); ++j)
         mbar_wait(&full[j % kStreamStages], static_cast<uint32_t>(j / kStreamStages) & 1u);
       return;
     }

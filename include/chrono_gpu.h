@@ -170,6 +170,13 @@ int cp_ctx_last_error(cp_ctx* ctx, char* buf, size_t len);
 /* Stream the *_device entry points use when passed NULL. */
 void* cp_ctx_stream(cp_ctx* ctx);
 int cp_ctx_synchronize(cp_ctx* ctx);
+/* Limit, in SM clock cycles, of every bounded device-side wait of this context's later
+ * launches (a CTA waiting for its staged frames; 0 = the default, 2^32 cycles, about 2 s).
+ * A wait that runs out makes its CTA leave (after its copies in flight have landed) and the
+ * call, or the next cp_ctx_synchronize, return CP_ERR_TIMEOUT; the context stays usable.
+ * A limit of 1 cycle gives up every wait at once (for tests of that path). No counterpart
+ * in the reference, whose loops have no device side. */
+int cp_ctx_set_wait_limit(cp_ctx* ctx, uint64_t cycles);
 /* Device memory owned by the context (counted against its HBM budget). */
 int cp_dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr);
 int cp_dev_free(cp_ctx* ctx, void* ptr);

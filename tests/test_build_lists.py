@@ -26,6 +26,16 @@ def test_batch_variants_match_build():
     assert _x_list("CP_BATCH_VARIANTS") == sorted(build.BATCH_VARIANTS)
 
 
+def test_pixel_thread_variants_match_build():
+    text = open(os.path.join(CSRC, "cp_internal.h")).read()
+    start = text.index("#define CP_PX_VARIANTS(X)")
+    body = text[start:text.index("\n#define", start + 1)]
+    listed = sorted(tuple(int(v) for v in t)
+                    for t in re.findall(r"X\((\d+), (\d+), (\d+)\)", body))
+    assert listed == sorted(build.PX_VARIANTS)
+    assert len(listed) == 12
+
+
 def test_every_rgb_outlier_setting_has_a_variant():
     """Every (distance kind, outlier group, background) an RGB stack can map to is compiled."""
     have = set(build.KERNEL_VARIANTS)

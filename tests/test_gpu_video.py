@@ -1,8 +1,9 @@
 """Chrono-video windows that slide by one frame (the sliding-window kernel) against the oracle
 (needs a GB300).
 
-Runs of equal-length windows, each the previous one shifted by one frame, take the kernel that
-keeps per-pixel histograms and walks the order statistics from window to window; the growing
+Runs of equal-length windows (2..64 frames), each the previous one shifted by one frame, take
+the kernel that keeps each pixel's window bit planes in registers and shifts one frame in per
+window; the growing
 and shrinking windows at the ends of a create_video sequence (src/main.rs:230-286) go to the
 batched kernel. Every window must equal the oracle's composite of that window alone: the
 composite and blend mask within 1 LSB per band (expected 0) and the warning count exact."""
@@ -76,8 +77,9 @@ def check(pool, wins, p, got):
 
 @pytest.mark.parametrize("L", [2, 3, 8, 31, 32, 33, 64, 65, 100, 128])
 def test_sliding_lengths(ctx, L):
-    """Window lengths across the 1, 2 and 4 flag-word kernels, odd and even (median pairs),
-    on a frame whose last 32-pixel tile is partial."""
+    """Window lengths of the one- and two-word plane kernels (2..64), odd and even (median
+    pairs), and longer windows (the batched kernel), on a frame whose last 32-pixel tile is
+    partial."""
     rng = np.random.default_rng(L)
     nwin = 7
     pool = cases.random_stack(rng, L + nwin - 1, 13, 37, 3, n_spots=6)
