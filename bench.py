@@ -16,6 +16,10 @@ Metric: megapixel-frames per second = 6 * 64 * 1920 * 1080 / 1e6 per step / time
               its mean launch time, against the measured HBM copy bandwidth
   cpu_baseline  the C++ restatement of the reference (oracle/) on the same whole stack, two
               steps on all host threads
+  batched     the batched half of the metric, against the plain kernel on the same work:
+              batched.video (300 resident 1080p frames, 269 sliding windows of 32) and
+              batched.serve (512 mixed jobs through the continuous-batching server, p50/p99
+              latency); --no-batched leaves them out
 
 --impl reference times the reference's CPU algorithm (the oracle restatement; the Rust
 reference cannot be built here) on the same workload, the whole stack for every step, and
@@ -435,6 +439,15 @@ def run_gpu(args):
         "clocks": clk_summary,
         "gpu_launches": args.steps * len(VARIANTS),
     }
+    if not args.no_batched:
+        # the batched half of the metric: the sliding-window chrono-video and served mixed
+        # jobs, each against the plain one-stack-per-launch kernel on the same work
+        line["batched"] = {}
+        for name, fn in (("video", video_workload), ("serve", serve_workload)):
+            try:
+                line["batched"][name] = fn(args, ctx, lib, _abi, local)
+            except Exception as e:  # the headline line is printed in any case
+                line["batched"][name] = {"error": "%s: %s" % (type(e).__name__, e)}
     print(json.dumps(line), flush=True)
 
 
@@ -577,24 +590,26 @@ def run_video(args):
 SERVE_RES = [(320, 240), (1280, 720), (1920, 1080), (4000, 3000)]
 
 
-def run_serve(args):
+def serve_workload(args, ctx, lib, _abi, local):
     """Mixed jobs through the continuous-batching server: 512 jobs, N ~ U{8..128},
     resolution ~ U{320x240, 1280x720, 1920x1080, 4000x3000}, outlier mode ~ U{extreme,
     average, first, last}, Poisson arrivals, 60 GB HBM budget. Job frames are drawn (by the
-    job's seed) from 16 pinned host frames per resolution, so the host side stays small;
-    every job still uploads its own N frames."""
+    job's seed) from 16 pinned host frames per resolution (generated on the device and read
+    back), so the host side stays small; every job still uploads its own N frames. Returns a
+    dict."""
     import numpy as np
     from chrono_photo_gb300 import example_data, make_params
     from chrono_photo_gb300.api import Server
-    ctx, lib, _abi, local = _ctx_and_lib()
     jobs = example_data.job_specs(seed=4, count=args.jobs)
     pool_n = 16
     pools = {}
     for (w, h) in SERVE_RES:
         ptr, arr = _pinned(ctx, lib, pool_n * w * h * C)
         arr = arr.reshape(pool_n, h, w, C)
-        example_data.stack(pool_n, w, h, sigma=3, n_disks=2, rmin=h / 40, rmax=h / 20,
-                           seed=4 + w, out=arr)
+        gen = example_data.stack_device(pool_n, w, h, sigma=3, n_disks=2, rmin=h / 40,
+                                        rmax=h / 20, seed=4 + w)
+        ctx.check(lib.cp_memcpy_d2h(ctx.handle, ptr, gen.data_ptr(), arr.nbytes, None))
+        del gen
         pools[(w, h)] = (ptr, arr)
     mpx_job = [j["n"] * j["w"] * j["h"] / 1e6 for j in jobs]
 
@@ -604,8 +619,10 @@ def run_serve(args):
 
     # kernel only: the same jobs with device-resident frames, 64 per batched launch
     dpool = {}
+    dev_allocs = []
     for key, (ptr, arr) in pools.items():
         d = ctx.alloc(arr.nbytes)
+        dev_allocs.append(d)
         ctx.check(lib.cp_memcpy_h2d(ctx.handle, d, ptr, arr.nbytes, None))
         dpool[key] = d
     keep = []
@@ -625,6 +642,7 @@ def run_serve(args):
             stacks[k] = _abi.Stack(n=j["n"], width=j["w"], height=j["h"], channels=C,
                                    frames=ct.cast(ptrs, ct.POINTER(ct.c_void_p)))
             outs[k] = ctx.alloc(fb)
+            dev_allocs.append(outs[k])
         prm = (_abi.Params * len(bj))(*[params[ji] for ji in bj])
         batches.append((stacks, prm, outs, len(bj)))
 
@@ -674,18 +692,19 @@ def run_serve(args):
         ids = []
         t0 = time.perf_counter()
         t_next = t0
-        with ClockSampler(local) as clk:
-            for j, g, prm in zip(jobs, gaps, params):
-                t_next += g
-                while time.perf_counter() < t_next:
-                    pass
-                ids.append(srv.submit(frames_of(j), params=prm))
-            res = [srv.wait(i) for i in ids]
+        for j, g, prm in zip(jobs, gaps, params):
+            t_next += g
+            while time.perf_counter() < t_next:
+                pass
+            ids.append(srv.submit(frames_of(j), params=prm))
+        res = [srv.wait(i) for i in ids]
         wall = max(r["done_s"] for r in res) - min(r["submit_s"] for r in res)
     lat = np.array([r["done_s"] - r["submit_s"] for r in res]) * 1e3
     bad = sum(1 for r in res if r["status"] != 0)
     h2d = sum(j["n"] * j["w"] * j["h"] * C for j in jobs)
-    print(json.dumps({
+    for d in dev_allocs:
+        ctx.free(d)
+    return {
         "workload": "serve", "metric": METRIC, "value": total_mpxf / wall, "unit": METRIC,
         "jobs": len(jobs), "failed": bad, "wall_s": wall,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
@@ -703,8 +722,15 @@ def run_serve(args):
         "e2e": {"value": total_mpxf / wall, "unit": METRIC, "h2d_bytes_total": h2d,
                 "d2h_bytes_total": 2 * sum(j["w"] * j["h"] * C for j in jobs)},
         "dtype": "u8", "data": "synthetic (seeded; frames drawn from 16 per resolution)",
-        "config": {"budget_gb": 60, "max_inflight": 8, "settings": "abs/0.05/0.2, background first"},
-        "clocks": clk.summary()}), flush=True)
+        "config": {"budget_gb": 60, "max_inflight": 8, "settings": "abs/0.05/0.2, background first"}}
+
+
+def run_serve(args):
+    ctx, lib, _abi, local = _ctx_and_lib()
+    with ClockSampler(local) as clk:
+        res = serve_workload(args, ctx, lib, _abi, local)
+    res["clocks"] = clk.summary()
+    print(json.dumps(res), flush=True)
 
 
 def run_shake(args):
@@ -863,6 +889,8 @@ def main():
                     choices=["hd", "video", "serve", "shake", "ingest"],
                     help="hd (default): the headline line; the others print their own lines")
     ap.add_argument("--jobs", type=int, default=512, help="serve: number of jobs")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="hd: leave out the video and serve sub-objects of the headline line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, _ = dist_env()
