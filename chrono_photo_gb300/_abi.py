@@ -20,6 +20,7 @@ CP_ERR_STATE = -7
 CP_ERR_NODEV = -8
 CP_ERR_LIMIT = -9
 CP_ERR_IO = -10
+CP_ERR_CANCELLED = -11
 
 MODE = {"outlier": 0, "darker": 1, "lighter": 2}
 OUTLIER = {"first": 0, "last": 1, "extreme": 2, "average": 3, "forward": 4, "backward": 5}
@@ -90,6 +91,7 @@ SIGNATURES = [
     ("cp_ctx_stream", P, [P]),
     ("cp_ctx_synchronize", ct.c_int, [P]),
     ("cp_ctx_set_wait_limit", ct.c_int, [P, U64]),
+    ("cp_ctx_fail_allocations", ct.c_int, [P, I32]),
     ("cp_dev_alloc", ct.c_int, [P, U64, ct.POINTER(P)]),
     ("cp_dev_free", ct.c_int, [P, P]),
     ("cp_host_alloc", ct.c_int, [P, U64, ct.POINTER(P)]),
@@ -115,6 +117,7 @@ SIGNATURES = [
     ("cp_server_create", ct.c_int, [P, U64, I32, ct.POINTER(P)]),
     ("cp_server_submit", ct.c_int, [P, ct.POINTER(Job), U64P]),
     ("cp_server_wait", ct.c_int, [P, U64, I32, ct.POINTER(JobResult)]),
+    ("cp_server_cancel", ct.c_int, [P, U64]),
     ("cp_server_destroy", ct.c_int, [P]),
     ("cp_png_info", ct.c_int, [P, ct.c_char_p, I32P, I32P, I32P]),
     ("cp_load_png", ct.c_int, [P, ct.POINTER(ct.c_char_p), I32, I32, P, U64, I32, I32, I32]),
@@ -135,7 +138,8 @@ STATUS_NAMES = {CP_OK: "ok", CP_ERR_ARG: "invalid argument", CP_ERR_OOM: "out of
                 CP_ERR_TIMEOUT: "timed out", CP_ERR_CUDA: "CUDA error",
                 CP_ERR_BUDGET: "HBM budget exceeded", CP_ERR_RANGE: "out of range",
                 CP_ERR_STATE: "invalid state", CP_ERR_NODEV: "no sm_103 device",
-                CP_ERR_LIMIT: "above a fixed limit", CP_ERR_IO: "image file error"}
+                CP_ERR_LIMIT: "above a fixed limit", CP_ERR_IO: "image file error",
+                CP_ERR_CANCELLED: "cancelled"}
 
 
 def lib():

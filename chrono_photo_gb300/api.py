@@ -508,6 +508,15 @@ class Server:
         return {"status": r.status, "warnings": r.warnings, "submit_s": r.submit_s,
                 "admit_s": r.admit_s, "done_s": r.done_s, "out": out, "blend": bl}
 
+    def cancel(self, job_id):
+        """Cancels a job still in the queue: True if cancelled (its wait() then reports status
+        CP_ERR_CANCELLED), False if it has already been admitted or has completed."""
+        rc = lib().cp_server_cancel(self.handle, job_id)
+        if rc == _abi.CP_ERR_STATE:
+            return False
+        self.ctx.check(rc, "cp_server_cancel")
+        return True
+
     def close(self):
         if self.handle:
             rc = lib().cp_server_destroy(self.handle)

@@ -55,7 +55,8 @@ int batch_group_key(const StackDev& d) { return (batch_variant_key(d) + 1) * 8 +
 // the specialised batched kernel when every stack takes the same one, else the general one.
 int launch_batch_dispatch(cp_ctx* ctx, const std::vector<StackDev>& host, const StackDev* d_stacks,
                           const int32_t* d_prefix, int32_t total, int32_t interleave,
-                          uint32_t* d_counter, int max_n, cudaStream_t st) {
+                          uint32_t* d_counter, int max_n, cudaStream_t st, uint32_t* d_err) {
+  uint32_t* err = d_err ? d_err : ctx->d_error;
   const int n = static_cast<int>(host.size());
   const int channels = host[0].channels;
   const int smem = smem_bytes_for(max_n, channels);
@@ -86,15 +87,15 @@ int launch_batch_dispatch(cp_ctx* ctx, const std::vector<StackDev>& host, const 
 #define CP_BATCH_LAUNCH(CH, K, G, B)                                                          \
   if (key == idx)                                                                             \
     rc = launch_batch_c##CH##_k##K##_g##G##_b##B(d_stacks, d_prefix, n, total, interleave,   \
-                                                 d_counter, ctx->d_error, grid, smem, st);   \
+                                                 d_counter, err, grid, smem, st);   \
   ++idx;
     CP_BATCH_VARIANTS(CP_BATCH_LAUNCH)
 #undef CP_BATCH_LAUNCH
   } else {
     switch (channels) {
-      case 1: rc = launch_batch_c1(d_stacks, d_prefix, n, total, interleave, d_counter, ctx->d_error, grid, smem, st); break;
-      case 3: rc = launch_batch_c3(d_stacks, d_prefix, n, total, interleave, d_counter, ctx->d_error, grid, smem, st); break;
-      default: rc = launch_batch_c4(d_stacks, d_prefix, n, total, interleave, d_counter, ctx->d_error, grid, smem, st); break;
+      case 1: rc = launch_batch_c1(d_stacks, d_prefix, n, total, interleave, d_counter, err, grid, smem, st); break;
+      case 3: rc = launch_batch_c3(d_stacks, d_prefix, n, total, interleave, d_counter, err, grid, smem, st); break;
+      default: rc = launch_batch_c4(d_stacks, d_prefix, n, total, interleave, d_counter, err, grid, smem, st); break;
     }
   }
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "batch launch");
@@ -106,7 +107,7 @@ static int batch_launch_raw(cp_ctx* ctx, BatchPlan& plan, int max_n, cudaStream_
   int32_t* d_prefix = reinterpret_cast<int32_t*>(d_stacks + n_stacks);
   uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + n_stacks + 1);
   return launch_batch_dispatch(ctx, plan.host, d_stacks, d_prefix, plan.total, plan.interleave,
-                               d_counter, max_n, st);
+                               d_counter, max_n, st, nullptr);
 }
 
 }  // namespace cp

@@ -421,7 +421,20 @@ void budget_release(cp_ctx* ctx, uint64_t bytes) {
   ctx->used = bytes > ctx->used ? 0 : ctx->used - bytes;
 }
 
+bool injected_alloc_failure(cp_ctx* ctx) {
+  if (!ctx) return false;
+  int left = ctx->fail_allocs.load();
+  while (left > 0) {
+    if (ctx->fail_allocs.compare_exchange_weak(left, left - 1)) {
+      ctx_error(ctx, "allocation failed (injected by cp_ctx_fail_allocations)");
+      return true;
+    }
+  }
+  return false;
+}
+
 int dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr) {
+  if (injected_alloc_failure(ctx)) return CP_ERR_OOM;
   if (!ptr) return CP_ERR_ARG;
   *ptr = nullptr;
   if (bytes == 0) return CP_OK;
@@ -477,6 +490,7 @@ int ensure_pinned(cp_ctx* ctx, PinnedBuffer& b, uint64_t bytes) {
   if (b.ptr) cudaFreeHost(b.ptr);
   b.ptr = nullptr;
   b.bytes = 0;
+  if (injected_alloc_failure(ctx)) return CP_ERR_OOM;
   cudaError_t e = cudaHostAlloc(&b.ptr, bytes, cudaHostAllocPortable);
   if (e != cudaSuccess) return cuda_status(ctx, e, "cudaHostAlloc");
   b.bytes = bytes;
@@ -513,6 +527,7 @@ const char* cp_status_str(int status) {
     case CP_ERR_STATE: return "invalid state";
     case CP_ERR_NODEV: return "no sm_103 device";
     case CP_ERR_LIMIT: return "request above the fixed limit of the allocation-free entry point";
+    case CP_ERR_CANCELLED: return "job cancelled";
     case CP_ERR_IO: return "image file missing, unreadable or unsupported";
     default: return "unknown status";
   }
@@ -701,6 +716,12 @@ int cp_ctx_synchronize(cp_ctx* ctx) {
   return check_device_error(ctx);
 }
 
+int cp_ctx_fail_allocations(cp_ctx* ctx, int32_t count) {
+  if (!ctx || count < 0) return CP_ERR_ARG;
+  ctx->fail_allocs.store(count);
+  return CP_OK;
+}
+
 int cp_ctx_set_wait_limit(cp_ctx* ctx, uint64_t cycles) {
   if (!ctx || cycles > (uint64_t(1) << 62)) return CP_ERR_ARG;
   ctx->wait_cycles = static_cast<int64_t>(cycles);
@@ -718,6 +739,7 @@ int cp_dev_free(cp_ctx* ctx, void* ptr) {
 int cp_host_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr) {
   if (!ctx || !ptr) return CP_ERR_ARG;
   cudaSetDevice(ctx->device);
+  if (injected_alloc_failure(ctx)) return CP_ERR_OOM;
   return cuda_status(ctx, cudaHostAlloc(ptr, bytes, cudaHostAllocPortable), "cudaHostAlloc");
 }
 int cp_host_free(cp_ctx* ctx, void* ptr) {

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdint>
 #include <map>
 #include <memory>
@@ -55,6 +57,7 @@ struct cp_ctx {
   std::map<std::pair<int, int>, int> occupancy;  // (kernel key, smem) -> CTAs per SM
   uint32_t* d_error = nullptr;               // device error flags of bounded waits
   int64_t wait_cycles = 0;                   // bounded-wait limit of launches (0: default)
+  std::atomic<int> fail_allocs{0};           // injected failures of the next allocations
   unsigned long long* d_warn = nullptr;      // device warning counter (host-staged calls)
   // host-staged composite: device copies of the frames and outputs, pinned staging
   cp::DevBuffer frames_dev, out_dev, blend_dev, dbg_dev;
@@ -76,6 +79,8 @@ int check_device_error(cp_ctx* ctx);
 int budget_reserve(cp_ctx* ctx, uint64_t bytes);
 void budget_release(cp_ctx* ctx, uint64_t bytes);
 int dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr);
+// true (and one injected failure used up) when the next allocation must fail
+bool injected_alloc_failure(cp_ctx* ctx);
 int dev_free(cp_ctx* ctx, void* ptr);
 int ensure_buffer(cp_ctx* ctx, DevBuffer& b, uint64_t bytes);
 int ensure_pinned(cp_ctx* ctx, PinnedBuffer& b, uint64_t bytes);
@@ -87,6 +92,7 @@ int batch_variant_key(const StackDev& d);
 int batch_group_key(const StackDev& d);  // stacks with equal keys share a launch
 int launch_batch_dispatch(cp_ctx* ctx, const std::vector<StackDev>& host, const StackDev* d_stacks,
                           const int32_t* d_prefix, int32_t total, int32_t interleave,
-                          uint32_t* d_counter, int max_n, cudaStream_t st);
+                          uint32_t* d_counter, int max_n, cudaStream_t st,
+                          uint32_t* d_err);  // null: the context's error flag
 
 }  // namespace cp

@@ -27,7 +27,11 @@ namespace {
 template <int NW, bool DB>
 constexpr int kPxMinCtas = NW == 1 ? 6 : (NW == 2 ? (DB ? 4 : 5) : 2);
 
-template <int KIND, int OG, int BG, int NW, bool DB>
+// PA: how phase A runs. 0: warps 0..2, word per lane, 4 byte positions per selection round;
+// 1: the same with 2 byte positions per round (fewer registers); 2: every warp builds the
+// planes of its own pixel's samples (no exchange, no idle warp, a quarter of each transpose
+// unused).
+template <int KIND, int OG, int BG, int NW, bool DB, int PA = 0>
 __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB>))
     k_outlier_px(const __grid_constant__ StackDev S, uint32_t* error) {
   constexpr int C = 3;
@@ -91,37 +95,54 @@ __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB>))
     }
     ph ^= 1u;
     // phase A: order statistics of word `warp` of every column
-    if (warp < 3) {
-      const Rows<C, false> rd{buf + 4 * C * lane, nullptr};
-      uint32_t plo, phi;
-      float wq[4];
-      word_order_stats<C, NW, false, KIND>(S, g, rd, warp, lane, plo, phi, wq);
-      A.lo[warp][lane] = plo;
-      A.hi[warp][lane] = phi;
-      if (!S.thr_abs) {
+    if (PA != 2) {
+      if (warp < 3) {
+        const Rows<C, false> rd{buf + 4 * C * lane, nullptr};
+        uint32_t plo, phi;
+        float wq[4];
+        word_order_stats<C, NW, false, KIND, (PA == 1 ? 2 : (NW <= 2 ? 4 : 2))>(
+            S, g, rd, warp, lane, plo, phi, wq);
+        A.lo[warp][lane] = plo;
+        A.hi[warp][lane] = phi;
+        if (!S.thr_abs) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) A.wq[4 * warp + k][lane] = wq[k];
+          for (int k = 0; k < 4; ++k) A.wq[4 * warp + k][lane] = wq[k];
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
     // phases B and C: pixel `warp` of column `lane`
     {
       const int p = warp;
       const int pin = 4 * lane + p;
       const int pix_idx = g.out_px0 + pin;
       const int q0 = 3 * p, wa = q0 >> 2, sh = 8 * (q0 & 3);
-      const uint32_t lo3 = __funnelshift_r(A.lo[wa][lane], A.lo[wa + 1][lane], sh) & 0x00FFFFFFu;
-      const uint32_t hi3 = __funnelshift_r(A.hi[wa][lane], A.hi[wa + 1][lane], sh) & 0x00FFFFFFu;
-      float wq3[C];
-#pragma unroll
-      for (int ch = 0; ch < C; ++ch) wq3[ch] = S.thr_abs ? 0.0f : A.wq[q0 + ch][lane];
-      const PxStat<C> st = px_stat<C>(S, lo3, hi3, wq3);
       // sample i of this pixel: bytes 12 * lane + 3 * p of row i (byte 3 unspecified)
       const uint32_t* col = reinterpret_cast<const uint32_t*>(buf) + 3 * lane + wa;
       auto load = [&](int i) -> uint32_t {
         const uint32_t* r = col + i * (kPitch<C> / 4);
         return __funnelshift_r(r[0], r[1], sh);
       };
+      uint32_t lo3, hi3;
+      float wq3[C];
+      if (PA == 2) {
+        float q1v[C], q3v[C];
+        pixel_order_stats<C, NW, KIND>(S, n, load, lo3, hi3, wq3, q1v, q3v);
+        if (pin < g.npx && (S.dbg_q1 || S.dbg_q3)) {
+#pragma unroll
+          for (int ch = 0; ch < C; ++ch) {
+            const size_t o = static_cast<size_t>(pix_idx) * C + ch;
+            if (S.dbg_q1) S.dbg_q1[o] = q1v[ch];
+            if (S.dbg_q3) S.dbg_q3[o] = q3v[ch];
+          }
+        }
+      } else {
+        lo3 = __funnelshift_r(A.lo[wa][lane], A.lo[wa + 1][lane], sh) & 0x00FFFFFFu;
+        hi3 = __funnelshift_r(A.hi[wa][lane], A.hi[wa + 1][lane], sh) & 0x00FFFFFFu;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) wq3[ch] = S.thr_abs ? 0.0f : A.wq[q0 + ch][lane];
+      }
+      const PxStat<C> st = px_stat<C>(S, lo3, hi3, wq3);
       uint32_t pb[NW];
       int32_t key;
       float dmax;
@@ -163,17 +184,25 @@ __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB>))
   flush_warnings(S.warnings, warn);
 }
 
+// Phase A per kind, as measured on the 64 x 1080p stack: word-column selection for integer
+// (abs) distances (0.293 ms vs 0.300 per-pixel), per-pixel planes for rel thresholds, whose
+// six selections per channel spill in the word-column layout (0.482 vs 0.517 ms).
+template <int KIND>
+constexpr int kPxPhaseA = KIND == kF32Kind ? 2 : 0;
+
 template <int KIND, int OG, int BG, int NW, bool DB>
 int px_launch_t(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
-  const void* fn = reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB>);
+  const void* fn =
+      reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB, kPxPhaseA<KIND>>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_outlier_px<KIND, OG, BG, NW, DB>
+  k_outlier_px<KIND, OG, BG, NW, DB, kPxPhaseA<KIND>>
       <<<grid, kPxThreads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
   return static_cast<int>(cudaGetLastError());
 }
 template <int KIND, int OG, int BG, int NW, bool DB>
 int px_occupancy_t(int smem) {
-  const void* fn = reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB>);
+  const void* fn =
+      reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB, kPxPhaseA<KIND>>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kPxThreads, smem) != cudaSuccess)

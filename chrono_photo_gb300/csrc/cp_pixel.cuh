@@ -52,6 +52,78 @@ DEVI PxStat<C> px_stat(const StackDev& S, uint32_t lo3, uint32_t hi3, const floa
   return r;
 }
 
+// Order statistics of one pixel from its own samples: bit planes of the C channel bytes of
+// each sample word (8x8 bit transposes of 8 samples, then a byte transpose of 4 groups),
+// radix selections of the median pair and, for rel thresholds, the quartiles
+// (src/chrono.rs:220-255). lo3 / hi3 as for px_stat; wq = w * iqr_inv; q1v / q3v the
+// quartiles (debug outputs).
+template <int C, int NW, int KIND, typename Load>
+DEVI void pixel_order_stats(const StackDev& S, int n, Load load, uint32_t& lo3, uint32_t& hi3,
+                            float (&wq)[C], float (&q1v)[C], float (&q3v)[C]) {
+  uint32_t P[C][8][NW];
+#pragma unroll
+  for (int blk = 0; blk < NW; ++blk) {
+    uint32_t a[4][8];
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      const int f0 = blk * 32 + g * 8;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) a[g][r] = (f0 + r < n) ? load(f0 + r) : 0u;
+      transpose8(a[g]);
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {  // 4x4 byte transpose: group g -> byte g
+      const uint32_t t0 = __byte_perm(a[0][r], a[1][r], 0x5140);
+      const uint32_t t1 = __byte_perm(a[0][r], a[1][r], 0x7362);
+      const uint32_t t2 = __byte_perm(a[2][r], a[3][r], 0x5140);
+      const uint32_t t3 = __byte_perm(a[2][r], a[3][r], 0x7362);
+      if (C > 0) P[0][r][blk] = __byte_perm(t0, t2, 0x5410);
+      if (C > 1) P[1 % C][r][blk] = __byte_perm(t0, t2, 0x7632);
+      if (C > 2) P[2 % C][r][blk] = __byte_perm(t1, t3, 0x5410);
+      if (C > 3) P[3 % C][r][blk] = __byte_perm(t1, t3, 0x7632);
+    }
+  }
+  uint32_t smask[NW];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
+  uint32_t lo[C], hi[C];
+  select_rank<NW, C>(P, smask, S.med_k, lo);
+  if (S.med_pair) {
+    select_rank<NW, C>(P, smask, S.med_k + 1, hi);
+  } else {
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) hi[ch] = lo[ch];
+  }
+  lo3 = 0u;
+  hi3 = 0u;
+#pragma unroll
+  for (int ch = 0; ch < C; ++ch) {
+    lo3 |= lo[ch] << (8 * ch);
+    hi3 |= hi[ch] << (8 * ch);
+    wq[ch] = 0.0f;
+    q1v[ch] = 0.0f;
+    q3v[ch] = 0.0f;
+  }
+  if (KIND != kIntKind && !S.thr_abs) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
+    uint32_t a1[C], b1[C], a3[C], b3[C];
+    select_rank<NW, C>(P, smask, S.q1_k, a1);
+    if (S.q1_pair) select_rank<NW, C>(P, smask, S.q1_k + 1, b1);
+    select_rank<NW, C>(P, smask, S.q3_k, a3);
+    if (S.q3_pair) select_rank<NW, C>(P, smask, S.q3_k + 1, b3);
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) {
+      const float q1 = quantile_value(a1[ch], S.q1_pair ? b1[ch] : a1[ch], S.q1_pair != 0, S.q1_frac);
+      const float q3 = quantile_value(a3[ch], S.q3_pair ? b3[ch] : a3[ch], S.q3_pair != 0, S.q3_frac);
+      float iqr = __fsub_rn(q3, q1);
+      if (iqr == 0.0f) iqr = 1.0f;
+      wq[ch] = __fmul_rn(S.w[ch], __fdiv_rn(1.0f, iqr));
+      const bool wt = (S.wmask >> ch) & 1u;
+      q1v[ch] = wt ? q1 : 0.0f;
+      q3v[ch] = wt ? q3 : 0.0f;
+    }
+  }
+}
+
 // Largest-distance bookkeeping is compiled in for the outlier groups that pick `extreme`.
 template <int OG>
 constexpr bool kKeepMax = OG == kOgAny || OG == kOgSingle;

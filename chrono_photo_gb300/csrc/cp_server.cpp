@@ -53,6 +53,7 @@ uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
 // Stream-ordered device memory from the server's pool, counted against the context budget.
 int pool_alloc(cp_ctx* ctx, cudaMemPool_t pool, uint64_t bytes, cudaStream_t st, void** p) {
   *p = nullptr;
+  if (injected_alloc_failure(ctx)) return CP_ERR_OOM;
   int rc = budget_reserve(ctx, bytes);
   if (rc) return rc;
   const cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, st);
@@ -245,7 +246,9 @@ int admit(cp_server* srv, Job* j) {
     srv->pinned_free.erase(it);
   } else {
     void* h = nullptr;
-    if (cudaHostAlloc(&h, j->stage_bytes, cudaHostAllocPortable) != cudaSuccess) return CP_ERR_OOM;
+    if (injected_alloc_failure(srv->ctx) ||
+        cudaHostAlloc(&h, j->stage_bytes, cudaHostAllocPortable) != cudaSuccess)
+      return CP_ERR_OOM;
     j->stage = static_cast<uint8_t*>(h);
   }
   j->state = 1;
@@ -344,10 +347,14 @@ int launch_jobs(cp_server* srv, std::vector<Job*>& batch) {
   StackDev* d_stacks = reinterpret_cast<StackDev*>(dp);
   int32_t* d_prefix = reinterpret_cast<int32_t*>(dp + sizeof(StackDev) * nb);
   uint32_t* d_counter = reinterpret_cast<uint32_t*>(d_prefix + nb + 1);
+  // this launch's own error flag (a bounded wait that gave up), read back with each job's
+  // results, so a failed tile fails exactly the jobs of this launch
+  uint32_t* d_err = d_counter + 1;
   cudaMemcpyAsync(dp, hp, sizeof(StackDev) * nb + sizeof(int32_t) * (nb + 1),
                   cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st);
   const int rc = launch_batch_dispatch(ctx, descs, d_stacks, d_prefix, prefix.back(), 0,
-                                       d_counter, max_n, st);
+                                       d_counter, max_n, st, d_err);
   if (rc) return rc;
   cudaEventRecord(slot->ev, st);
   slot->busy = true;
@@ -356,6 +363,8 @@ int launch_jobs(cp_server* srv, std::vector<Job*>& batch) {
   for (Job* j : batch) {
     const uint64_t ob = out_bytes_of(*j);
     cudaMemcpyAsync(j->stage, j->out_dev, 2 * ob + 8, cudaMemcpyDeviceToHost, srv->d2h);
+    cudaMemcpyAsync(j->stage + 2 * ob + 8, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                    srv->d2h);
     cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming);
     cudaEventRecord(j->done_ev, srv->d2h);
     j->state = 2;
@@ -462,8 +471,11 @@ void worker_loop(cp_server* srv) {
         if (j->spec.out_blend && j->spec.params.mode == CP_MODE_OUTLIER)
           std::memcpy(j->spec.out_blend, j->stage + ob, bytes);
         std::memcpy(&j->res.warnings, j->stage + 2 * ob, 8);
+        uint32_t dev_err = 0;
+        std::memcpy(&dev_err, j->stage + 2 * ob + 8, sizeof dev_err);
         release(srv, j);
-        j->res.status = CP_OK;
+        // a tile of this job's launch gave up waiting for its frames: the output is partial
+        j->res.status = dev_err ? CP_ERR_TIMEOUT : CP_OK;
         j->res.done_s = now_s();
         j->state = 3;
         it = srv->active.erase(it);
@@ -579,6 +591,26 @@ int cp_server_wait(cp_server* srv, uint64_t job_id, int32_t timeout_ms, cp_job_r
   }
   *res = j->res;
   srv->jobs.erase(it);
+  return CP_OK;
+}
+
+int cp_server_cancel(cp_server* srv, uint64_t job_id) {
+  if (!srv) return CP_ERR_ARG;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  auto it = srv->jobs.find(job_id);
+  if (it == srv->jobs.end()) return CP_ERR_ARG;
+  Job* j = it->second.get();
+  if (j->state != 0) return CP_ERR_STATE;  // admitted or done: it runs to completion
+  for (auto q = srv->queue.begin(); q != srv->queue.end(); ++q)
+    if (*q == j) {
+      srv->queue.erase(q);
+      break;
+    }
+  j->res.status = CP_ERR_CANCELLED;
+  j->res.done_s = now_s();
+  j->state = 3;
+  srv->cv_done.notify_all();
+  srv->cv_work.notify_all();
   return CP_OK;
 }
 

@@ -564,10 +564,10 @@ DEVI bool og_is(const StackDev& S, int og) {
 // (2)+(3) of a tile: bit planes of word wp of column t and the order statistics of its 4
 // byte positions: plo / phi = d[k], d[k+1] of the median per byte (d[k] twice without a pair),
 // and for rel thresholds wq[k] = w * iqr_inv (src/chrono.rs:220-255) and the debug quartiles.
-template <int C, int NW, bool SH, int KIND>
+template <int C, int NW, bool SH, int KIND, int BPR = (NW <= 2 ? 4 : 2)>
 DEVI void word_order_stats(const StackDev& S, const TileGeo& g, const Rows<C, SH>& rd, int wp,
                            int t, uint32_t& plo_out, uint32_t& phi_out, float (&wq_out)[4]) {
-  constexpr int BP = NW <= 2 ? 4 : 2;  // byte positions per plane build (register budget)
+  constexpr int BP = BPR;  // byte positions per plane build (register budget)
   const int n = S.n;
   uint32_t smask[NW];
 #pragma unroll

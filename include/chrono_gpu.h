@@ -45,6 +45,7 @@ extern "C" {
 #define CP_ERR_NODEV (-8)   /* no CUDA device with compute capability 10.3                 */
 #define CP_ERR_LIMIT (-9)   /* request above a fixed limit (batch_static, composite_multi) */
 #define CP_ERR_IO (-10)     /* image file missing, unreadable or not a supported PNG       */
+#define CP_ERR_CANCELLED (-11) /* server job cancelled before it started                   */
 
 /* ---- option enums (src/options.rs) --------------------------------------------------- */
 /* SelectionMode, src/options.rs:8-31 */
@@ -177,6 +178,10 @@ int cp_ctx_synchronize(cp_ctx* ctx);
  * A limit of 1 cycle gives up every wait at once (for tests of that path). No counterpart
  * in the reference, whose loops have no device side. */
 int cp_ctx_set_wait_limit(cp_ctx* ctx, uint64_t cycles);
+/* Testing aid: the next `count` device or pinned allocations made for this context (its own
+ * buffers, cp_dev_alloc, cp_host_alloc, server jobs) fail with CP_ERR_OOM as if memory ran
+ * out; 0 cancels what is left. No counterpart in the reference. */
+int cp_ctx_fail_allocations(cp_ctx* ctx, int32_t count);
 /* Device memory owned by the context (counted against its HBM budget). */
 int cp_dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr);
 int cp_dev_free(cp_ctx* ctx, void* ptr);
@@ -334,6 +339,11 @@ int cp_server_submit(cp_server* srv, const cp_job* job, uint64_t* job_id);
 /* Waits up to timeout_ms (-1 = forever; 0 = poll without blocking) for job_id.
  * CP_ERR_TIMEOUT if not done yet. */
 int cp_server_wait(cp_server* srv, uint64_t job_id, int32_t timeout_ms, cp_job_result* res);
+/* Cancels a job that is still queued (not yet admitted): it completes at once with status
+ * CP_ERR_CANCELLED and its buffers are not touched. CP_ERR_STATE if the job has already been
+ * admitted or has completed (it then runs to completion), CP_ERR_ARG for an unknown id.
+ * The reference's processors run to completion; there is no counterpart. */
+int cp_server_cancel(cp_server* srv, uint64_t job_id);
 /* Stops accepting jobs, drains the queue and joins the worker. */
 int cp_server_destroy(cp_server* srv);
 

@@ -68,3 +68,33 @@ def test_wait_limit_arguments(ctx):
     assert lib.cp_ctx_set_wait_limit(None, 5) == _abi.CP_ERR_ARG
     assert lib.cp_ctx_set_wait_limit(ctx.handle, 1 << 63) == _abi.CP_ERR_ARG
     assert lib.cp_ctx_set_wait_limit(ctx.handle, 0) == _abi.CP_OK
+
+
+def test_injected_allocation_failure(ctx):
+    """A host-memory composite whose staging allocation fails reports CP_ERR_OOM, device and
+    pinned allocations fail the same way, and the next call on the same context succeeds
+    (the context's buffers are grown again on demand). A fresh context: its staging buffers
+    do not exist yet, so the composite has to allocate."""
+    rng = np.random.default_rng(4)
+    frames = cases.random_stack(rng, 30, 60, 80, 3, n_spots=4)
+    p = cases.params(mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+                     background="first")
+    lib = _abi.lib()
+    with cg.Context(0) as c2:
+        assert lib.cp_ctx_fail_allocations(c2.handle, 1) == _abi.CP_OK
+        try:
+            with pytest.raises(cg.ChronoError) as e:
+                c2.composite(frames, p)
+            assert e.value.status == _abi.CP_ERR_OOM
+            assert lib.cp_ctx_fail_allocations(c2.handle, 2) == _abi.CP_OK
+            with pytest.raises(cg.ChronoError) as e:
+                c2.alloc(1024)
+            assert e.value.status == _abi.CP_ERR_OOM
+            ptr = ct.c_void_p()
+            assert lib.cp_host_alloc(c2.handle, 4096, ct.byref(ptr)) == _abi.CP_ERR_OOM
+        finally:
+            assert lib.cp_ctx_fail_allocations(c2.handle, 0) == _abi.CP_OK
+        assert lib.cp_ctx_fail_allocations(c2.handle, -1) == _abi.CP_ERR_ARG
+        got = c2.composite(frames, p)
+    ref = oracle.composite(frames, p)
+    cases.assert_close_u8(got[0], ref[0], what="after an injected failure")

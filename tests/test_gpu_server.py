@@ -72,3 +72,52 @@ def test_invalid_job_rejected(ctx):
     with cg.Server(ctx) as srv:
         with pytest.raises(_abi.ChronoError):
             srv.submit(np.zeros((2, 4, 4, 3), np.uint8), cases.params(threshold="rel/1/2"))
+
+
+def test_cancel_queued_jobs(ctx):
+    """With one job in flight at a time, jobs still in the queue can be cancelled: they
+    complete with CP_ERR_CANCELLED and the others are unaffected."""
+    rng = np.random.default_rng(12)
+    frames = [cases.random_stack(rng, 40, 64, 96, 3, n_spots=4) for _ in range(8)]
+    p = cases.params(mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+                     background="first")
+    with cg.Server(ctx, max_inflight=1) as srv:
+        ids = [srv.submit(f, p) for f in frames]
+        cancelled = [srv.cancel(i) for i in ids[4:]]
+        res = [srv.wait(i) for i in ids]
+    assert any(cancelled)
+    for f, r, c in zip(frames, res, [False] * 4 + cancelled):
+        if c:
+            assert r["status"] == _abi.CP_ERR_CANCELLED
+        else:
+            assert r["status"] == 0
+            ref = oracle.composite(f, p)
+            cases.assert_close_u8(r["out"], ref[0], what="served composite")
+
+
+def test_server_reports_timeouts_and_allocation_failures(ctx):
+    """A launch whose bounded waits give up fails exactly its jobs with CP_ERR_TIMEOUT; an
+    injected allocation failure fails the job being admitted with CP_ERR_OOM; jobs after
+    either run normally on the same server."""
+    rng = np.random.default_rng(13)
+    frames = cases.random_stack(rng, 20, 48, 64, 3, n_spots=3)
+    p = cases.params(mode="outlier", threshold="abs/0.05/0.2", outlier="average",
+                     background="first")
+    ref = oracle.composite(frames, p)
+    lib = _abi.lib()
+    with cg.Server(ctx, max_inflight=2) as srv:
+        assert lib.cp_ctx_set_wait_limit(ctx.handle, 1) == 0
+        try:
+            r = srv.wait(srv.submit(frames, p))
+        finally:
+            assert lib.cp_ctx_set_wait_limit(ctx.handle, 0) == 0
+        assert r["status"] == _abi.CP_ERR_TIMEOUT
+        assert lib.cp_ctx_fail_allocations(ctx.handle, 1) == 0
+        try:
+            r = srv.wait(srv.submit(frames, p))
+        finally:
+            assert lib.cp_ctx_fail_allocations(ctx.handle, 0) == 0
+        assert r["status"] == _abi.CP_ERR_OOM
+        r = srv.wait(srv.submit(frames, p))
+        assert r["status"] == 0
+        cases.assert_close_u8(r["out"], ref[0], what="after failures")
