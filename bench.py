@@ -20,6 +20,8 @@ Metric: megapixel-frames per second = 6 * 64 * 1920 * 1080 / 1e6 per step / time
               batched.video (300 resident 1080p frames, 269 sliding windows of 32) and
               batched.serve (512 mixed jobs through the continuous-batching server, p50/p99
               latency); --no-batched leaves them out
+  autotune    the launch configuration the autotuner chose per outlier setting (phase A
+              layout, staging buffers, CTAs per SM) with the tuned and static times
 
 --impl reference times the reference's CPU algorithm (the oracle restatement; the Rust
 reference cannot be built here) on the same workload, the whole stack for every step, and
@@ -438,6 +440,7 @@ def run_gpu(args):
                          "kind": "port", "sample": cpu_desc},
         "clocks": clk_summary,
         "gpu_launches": args.steps * len(VARIANTS),
+        "autotune": tuning_report(ctx, lib, _abi),
     }
     if not args.no_batched:
         # the batched half of the metric: the sliding-window chrono-video and served mixed
@@ -449,6 +452,19 @@ def run_gpu(args):
             except Exception as e:  # the headline line is printed in any case
                 line["batched"][name] = {"error": "%s: %s" % (type(e).__name__, e)}
     print(json.dumps(line), flush=True)
+
+
+def tuning_report(ctx, lib, _abi):
+    """The launch configurations the autotuner chose for the outlier settings of this run
+    (cp_ctx_tuning_report): per key the tuned and the static configuration's times, measured
+    on the first launch of the warm-up or read from the tuning cache."""
+    buf = ct.create_string_buffer(1 << 16)
+    ctx.check(lib.cp_ctx_tuning_report(ctx.handle, buf, len(buf)), "cp_ctx_tuning_report")
+    rows = json.loads(buf.value.decode())
+    for r in rows:
+        r["tuned_over_static"] = (r["static_ms"] / r["tuned_ms"]) if r["tuned_ms"] else None
+    return {"keys": rows, "env": {k: os.environ.get(k) for k in ("CP_AUTOTUNE", "CP_PX_CONFIG")
+                                  if os.environ.get(k) is not None}}
 
 
 # ---- other configurations (--workload): their own JSON lines, not the headline ---------------
@@ -701,12 +717,16 @@ def serve_workload(args, ctx, lib, _abi, local):
         wall = max(r["done_s"] for r in res) - min(r["submit_s"] for r in res)
     lat = np.array([r["done_s"] - r["submit_s"] for r in res]) * 1e3
     bad = sum(1 for r in res if r["status"] != 0)
+    bad_status = {}
+    for r in res:
+        if r["status"] != 0:
+            bad_status[str(r["status"])] = bad_status.get(str(r["status"]), 0) + 1
     h2d = sum(j["n"] * j["w"] * j["h"] * C for j in jobs)
     for d in dev_allocs:
         ctx.free(d)
     return {
         "workload": "serve", "metric": METRIC, "value": total_mpxf / wall, "unit": METRIC,
-        "jobs": len(jobs), "failed": bad, "wall_s": wall,
+        "jobs": len(jobs), "failed": bad, "failed_status": bad_status, "wall_s": wall,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "max": float(lat.max())},
         "arrival_mean_gap_ms": mean_gap * 1e3,

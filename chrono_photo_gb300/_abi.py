@@ -92,6 +92,7 @@ SIGNATURES = [
     ("cp_ctx_synchronize", ct.c_int, [P]),
     ("cp_ctx_set_wait_limit", ct.c_int, [P, U64]),
     ("cp_ctx_fail_allocations", ct.c_int, [P, I32]),
+    ("cp_ctx_tuning_report", ct.c_int, [P, ct.c_char_p, ct.c_size_t]),
     ("cp_dev_alloc", ct.c_int, [P, U64, ct.POINTER(P)]),
     ("cp_dev_free", ct.c_int, [P, P]),
     ("cp_host_alloc", ct.c_int, [P, U64, ct.POINTER(P)]),

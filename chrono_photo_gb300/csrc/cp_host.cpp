@@ -297,45 +297,9 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
     return cuda_status(ctx, static_cast<cudaError_t>(rc), "simple launch");
   }
   if (d.mode == CP_MODE_OUTLIER && d.channels == 3 && !d.shifted && !d.has_crop &&
-      (d.fast_int || d.pair_f32)) {
-    // the pixel-thread kernel (cp_outlier_px.cuh), single-buffered staging (measured faster
-    // than double buffering, which costs a resident CTA per SM); CP_PX_BUFFERS=2 selects
-    // double buffering up to 64 frames
-    int k, g, b;
-    outlier_variant(d, &k, &g, &b);
-    const char* nb = std::getenv("CP_PX_BUFFERS");
-    const bool db = d.nw <= 2 && nb && std::strcmp(nb, "2") == 0;
-    const int psmem = px_smem_bytes(d.n, db);
-    if (psmem <= ctx->max_smem) {
-      const auto key = std::make_pair(4000 + 64 * k + 8 * g + 2 * b + (db ? 1 : 0), psmem);
-      int per_sm = 0, rc = -1;
-      {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        auto it = ctx->occupancy.find(key);
-        if (it != ctx->occupancy.end()) per_sm = it->second;
-      }
-      if (per_sm == 0) {
-#define CP_PX_OCC(K, G, B)                                                               \
-  if (k == K && g == G && b == B)                                                        \
-    per_sm = px_launch_k##K##_g##G##_b##B(d, db, true, 0, psmem, nullptr, nullptr);
-        CP_PX_VARIANTS(CP_PX_OCC)
-#undef CP_PX_OCC
-        if (per_sm < 1) per_sm = 1;
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        ctx->occupancy[key] = per_sm;
-      }
-      const int grid = std::max(1, std::min(d.tiles, per_sm * ctx->sm_count));
-#define CP_PX_RUN(K, G, B)                                                               \
-  if (k == K && g == G && b == B)                                                        \
-    rc = px_launch_k##K##_g##G##_b##B(d, db, false, grid, psmem, stream, ctx->d_error);
-      CP_PX_VARIANTS(CP_PX_RUN)
-#undef CP_PX_RUN
-      if (rc < 0) {
-        ctx_error(ctx, "no pixel-thread kernel for variant %d/%d/%d", k, g, b);
-        return CP_ERR_ARG;
-      }
-      return cuda_status(ctx, static_cast<cudaError_t>(rc), "composite launch");
-    }
+      (d.fast_int || d.pair_f32) && px_smem_bytes(d.n, false) <= ctx->max_smem) {
+    // the pixel-thread kernel (cp_outlier_px.cuh), configured by cp_tune.cpp
+    return launch_px(ctx, d, stream);
   }
   const int smem = smem_bytes_for(d.n, d.channels);
   if (smem > ctx->max_smem) {
@@ -663,6 +627,7 @@ int cp_ctx_create(int32_t device, uint64_t hbm_budget, cp_ctx** out) {
   ctx->device = device;
   ctx->budget = hbm_budget;
   ctx->sm_count = prop.multiProcessorCount;
+  ctx->gpu_name = prop.name;
   ctx->max_smem = static_cast<int>(prop.sharedMemPerBlockOptin);
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||

@@ -38,6 +38,16 @@ struct BatchPlan {
   int32_t max_n = 0;
 };
 
+// Launch configuration of the pixel-thread outlier kernel (cp_tune.cpp).
+struct PxChoice {
+  int pa = -1;    // phase A: 0 word columns, 2 per pixel, -1 the static choice of the kind
+  int db = 0;     // 1: two staging buffers per CTA
+  int ctas = 0;   // CTAs per SM (0: as many as fit)
+  float ms = 0.0f, static_ms = 0.0f;  // measured launch times: this choice, the static one
+  std::string name;
+  bool from_cache = false;
+};
+
 }  // namespace cp
 
 struct cp_ctx {
@@ -58,6 +68,10 @@ struct cp_ctx {
   uint32_t* d_error = nullptr;               // device error flags of bounded waits
   int64_t wait_cycles = 0;                   // bounded-wait limit of launches (0: default)
   std::atomic<int> fail_allocs{0};           // injected failures of the next allocations
+  std::string gpu_name;                      // device name (tuning cache key)
+  std::map<int, cp::PxChoice> px_tuned;      // pixel-thread kernel choices by key
+  bool tune_loaded = false;                  // the tuning cache file has been read
+  std::mutex tune_mu;                        // one tuning run at a time
   unsigned long long* d_warn = nullptr;      // device warning counter (host-staged calls)
   // host-staged composite: device copies of the frames and outputs, pinned staging
   cp::DevBuffer frames_dev, out_dev, blend_dev, dbg_dev;
@@ -75,6 +89,8 @@ int fade_lut(const cp_fade* f, int32_t n, int32_t frame_offset, float* out);
 int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
                   const uint8_t* const* dev_frames, StackDev* d);
 int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream);
+// The pixel-thread kernel with its measured (or cached, forced, static) configuration.
+int launch_px(cp_ctx* ctx, const StackDev& d, cudaStream_t stream);
 int check_device_error(cp_ctx* ctx);
 int budget_reserve(cp_ctx* ctx, uint64_t bytes);
 void budget_release(cp_ctx* ctx, uint64_t bytes);

@@ -183,13 +183,14 @@ inline int px_smem_bytes(int n, bool db) {
   return kSmemHeader + (db ? 2 : 1) * n * row_pitch_host(3) + static_cast<int>(sizeof(PxAux));
 }
 // (distance kind, outlier group, background) of the compiled pixel-thread kernels; each
-// translation unit holds plane-word counts 1, 2 (single and double buffered) and 4 (single).
+// translation unit holds plane-word counts 1 and 2 (single and double buffered) and 4
+// (single), each with phase A by word column (pa 0) and by pixel (pa 2).
 #define CP_PX_VARIANTS(X)                                                                    \
   X(1, 1, 1) X(1, 2, 1) X(1, 3, 1) X(1, 1, 0) X(1, 2, 0) X(1, 3, 0) X(2, 1, 1) X(2, 2, 1)  \
   X(2, 3, 1) X(2, 1, 0) X(2, 2, 0) X(2, 3, 0)
 #define CP_DECLARE_PX(K, G, B)                                                               \
-  int px_launch_k##K##_g##G##_b##B(const StackDev& s, bool db, bool occupancy_only, int grid, \
-                                   int smem, void* stream, uint32_t* error);
+  int px_launch_k##K##_g##G##_b##B(const StackDev& s, int pa, bool db, bool occupancy_only,   \
+                                   int grid, int smem, void* stream, uint32_t* error);
 CP_PX_VARIANTS(CP_DECLARE_PX)
 #undef CP_DECLARE_PX
 

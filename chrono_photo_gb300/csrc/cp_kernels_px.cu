@@ -14,10 +14,10 @@
 
 namespace cp {
 
-int CP_PCAT(px_launch_k, CP_KIND, _g, CP_OG, _b, CP_BG)(const StackDev& s, bool db,
+int CP_PCAT(px_launch_k, CP_KIND, _g, CP_OG, _b, CP_BG)(const StackDev& s, int pa, bool db,
                                                        bool occupancy_only, int grid, int smem,
                                                        void* stream, uint32_t* error) {
-  return px_dispatch<CP_KIND, CP_OG, CP_BG>(s, db, occupancy_only, grid, smem, stream, error);
+  return px_dispatch<CP_KIND, CP_OG, CP_BG>(s, pa, db, occupancy_only, grid, smem, stream, error);
 }
 
 }  // namespace cp

@@ -184,25 +184,24 @@ __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB>))
   flush_warnings(S.warnings, warn);
 }
 
-// Phase A per kind, as measured on the 64 x 1080p stack: word-column selection for integer
-// (abs) distances (0.293 ms vs 0.300 per-pixel), per-pixel planes for rel thresholds, whose
-// six selections per channel spill in the word-column layout (0.482 vs 0.517 ms).
+// Static phase-A choice per kind (what the autotuner starts from), as measured on the
+// 64 x 1080p stack: word-column selection for integer (abs) distances (0.293 ms vs 0.300
+// per-pixel), per-pixel planes for rel thresholds, whose six selections per channel spill in
+// the word-column layout (0.482 vs 0.517 ms).
 template <int KIND>
 constexpr int kPxPhaseA = KIND == kF32Kind ? 2 : 0;
 
-template <int KIND, int OG, int BG, int NW, bool DB>
+template <int KIND, int OG, int BG, int NW, bool DB, int PA>
 int px_launch_t(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {
-  const void* fn =
-      reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB, kPxPhaseA<KIND>>);
+  const void* fn = reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB, PA>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_outlier_px<KIND, OG, BG, NW, DB, kPxPhaseA<KIND>>
+  k_outlier_px<KIND, OG, BG, NW, DB, PA>
       <<<grid, kPxThreads, smem, static_cast<cudaStream_t>(stream)>>>(s, error);
   return static_cast<int>(cudaGetLastError());
 }
-template <int KIND, int OG, int BG, int NW, bool DB>
+template <int KIND, int OG, int BG, int NW, bool DB, int PA>
 int px_occupancy_t(int smem) {
-  const void* fn =
-      reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB, kPxPhaseA<KIND>>);
+  const void* fn = reinterpret_cast<const void*>(&k_outlier_px<KIND, OG, BG, NW, DB, PA>);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kPxThreads, smem) != cudaSuccess)
@@ -210,19 +209,27 @@ int px_occupancy_t(int smem) {
   return blocks < 1 ? 1 : blocks;
 }
 
-// Launch (occupancy_only: CTAs per SM instead) of the variant for s.nw and db.
+// Launch (occupancy_only: CTAs per SM instead) of the variant for s.nw, phase-A mode pa
+// (0 word-column, 2 per-pixel; -1 the static choice of the kind) and staging buffers db.
 template <int KIND, int OG, int BG>
-int px_dispatch(const StackDev& s, bool db, bool occupancy_only, int grid, int smem, void* stream,
-                uint32_t* error) {
-#define CP_PX_CASE(NW, DBV)                                                               \
-  if (s.nw == NW && db == DBV)                                                            \
-    return occupancy_only ? px_occupancy_t<KIND, OG, BG, NW, DBV>(smem)                   \
-                          : px_launch_t<KIND, OG, BG, NW, DBV>(s, grid, smem, stream, error);
-  CP_PX_CASE(1, true)
-  CP_PX_CASE(1, false)
-  CP_PX_CASE(2, true)
-  CP_PX_CASE(2, false)
-  CP_PX_CASE(4, false)
+int px_dispatch(const StackDev& s, int pa, bool db, bool occupancy_only, int grid, int smem,
+                void* stream, uint32_t* error) {
+  if (pa < 0) pa = kPxPhaseA<KIND>;
+#define CP_PX_CASE(NW, DBV, PAV)                                                          \
+  if (s.nw == NW && db == DBV && pa == PAV)                                               \
+    return occupancy_only                                                                 \
+               ? px_occupancy_t<KIND, OG, BG, NW, DBV, PAV>(smem)                         \
+               : px_launch_t<KIND, OG, BG, NW, DBV, PAV>(s, grid, smem, stream, error);
+  CP_PX_CASE(1, false, 0)
+  CP_PX_CASE(1, false, 2)
+  CP_PX_CASE(1, true, 0)
+  CP_PX_CASE(1, true, 2)
+  CP_PX_CASE(2, false, 0)
+  CP_PX_CASE(2, false, 2)
+  CP_PX_CASE(2, true, 0)
+  CP_PX_CASE(2, true, 2)
+  CP_PX_CASE(4, false, 0)
+  CP_PX_CASE(4, false, 2)
 #undef CP_PX_CASE
   return -1;
 }

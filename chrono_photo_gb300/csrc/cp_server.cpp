@@ -109,6 +109,7 @@ struct LaunchSlot {
   uint64_t bytes = 0;
   void* pinned = nullptr;       // host staging of the descriptors
   cudaEvent_t ev = nullptr;     // launch finished
+  cudaEvent_t freed = nullptr;  // the results and the error word of the launch read back
   bool busy = false;
 };
 
@@ -302,7 +303,7 @@ int launch_jobs(cp_server* srv, std::vector<Job*>& batch) {
   cp_ctx* ctx = srv->ctx;
   LaunchSlot* slot = nullptr;
   for (auto& s : srv->slots)
-    if (!s.busy || cudaEventQuery(s.ev) == cudaSuccess) {
+    if (!s.busy || cudaEventQuery(s.freed) == cudaSuccess) {
       slot = &s;
       break;
     }
@@ -369,6 +370,10 @@ int launch_jobs(cp_server* srv, std::vector<Job*>& batch) {
     cudaEventRecord(j->done_ev, srv->d2h);
     j->state = 2;
   }
+  // the slot's memory (descriptors, counter, error word) is reused only after the d2h
+  // stream has read the error word: a reuse that only waited for the launch could overwrite
+  // it with the next launch's descriptors before this launch's jobs read it
+  cudaEventRecord(slot->freed, srv->d2h);
   return CP_OK;
 }
 
@@ -524,7 +529,10 @@ int cp_server_create(cp_ctx* ctx, uint64_t hbm_budget, int32_t max_inflight, cp_
   uint64_t keep = ~0ull;  // keep freed memory in the pool for later jobs (the budget bounds it)
   cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   srv->slots.resize(static_cast<size_t>(kStreams) * 2);
-  for (auto& s : srv->slots) cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming);
+  for (auto& s : srv->slots) {
+    cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&s.freed, cudaEventDisableTiming);
+  }
   srv->worker = std::thread(worker_loop, srv.get());
   *out = srv.release();
   return CP_OK;
@@ -636,6 +644,7 @@ int cp_server_destroy(cp_server* srv) {
     if (s.dev) dev_free(srv->ctx, s.dev);
     if (s.pinned) cudaFreeHost(s.pinned);
     cudaEventDestroy(s.ev);
+    cudaEventDestroy(s.freed);
   }
   for (auto& kv : srv->pinned_free) cudaFreeHost(kv.second);
   for (auto& s : srv->compute) cudaStreamDestroy(s);

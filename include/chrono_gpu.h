@@ -182,6 +182,15 @@ int cp_ctx_set_wait_limit(cp_ctx* ctx, uint64_t cycles);
  * buffers, cp_dev_alloc, cp_host_alloc, server jobs) fail with CP_ERR_OOM as if memory ran
  * out; 0 cancels what is left. No counterpart in the reference. */
 int cp_ctx_fail_allocations(cp_ctx* ctx, int32_t count);
+/* The launch configurations the context's autotuner chose for the single-stack outlier
+ * kernel, as a JSON array (one object per distance kind, outlier group, background and
+ * plane-word count: the choice, its measured time and the static choice's time). The first
+ * launch of such a key on a stack that fills the GPU several times times every candidate
+ * configuration (results do not depend on it) and caches the fastest in a file keyed by GPU
+ * and library version (CP_TUNE_CACHE; CP_AUTOTUNE=0 turns tuning off). CP_ERR_LIMIT if the
+ * text did not fit `len`. Replaces the reference's hand-set thread counts
+ * (src/main.rs:49-54, :254-261). */
+int cp_ctx_tuning_report(cp_ctx* ctx, char* buf, size_t len);
 /* Device memory owned by the context (counted against its HBM budget). */
 int cp_dev_alloc(cp_ctx* ctx, uint64_t bytes, void** ptr);
 int cp_dev_free(cp_ctx* ctx, void* ptr);

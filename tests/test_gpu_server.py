@@ -40,6 +40,32 @@ def test_results_same_alone_and_in_mix(ctx):
         assert r["submit_s"] <= r["admit_s"] <= r["done_s"]
 
 
+def test_many_launches_all_succeed(ctx):
+    """Hundreds of jobs in bursts, so that launch slots are reused while the results of their
+    previous launches are still being read back, with batches of varying size (descriptor
+    arrays of varying length in the reused slot memory): every job succeeds with the result
+    of its lone composite."""
+    rng = np.random.default_rng(5)
+    base = [cases.random_stack(rng, 40, 120, 160, 3, n_spots=4) for _ in range(4)]
+    specs = []
+    for i in range(240):
+        n = int(rng.integers(3, 40))
+        specs.append((i % 4, n, MODES[i % 4]))
+    alone = {}
+    for b, n, kw in specs:
+        if (b, n, kw["outlier"]) not in alone:
+            alone[(b, n, kw["outlier"])] = ctx.composite(base[b][:n], cases.params(**kw))[0]
+    with cg.Server(ctx, max_inflight=8) as srv:
+        ids, done = [], {}
+        for k in range(0, len(specs), 24):
+            ids += [srv.submit(base[b][:n], cases.params(**kw)) for b, n, kw in specs[k:k + 24]]
+            done[ids[-1]] = srv.wait(ids[-1])  # the burst's last job: the others mostly done
+        res = [done[j] if j in done else srv.wait(j) for j in ids]
+    assert [r["status"] for r in res] == [0] * len(specs)
+    for (b, n, kw), r in zip(specs, res):
+        assert np.array_equal(r["out"], alone[(b, n, kw["outlier"])])
+
+
 def test_shared_keyed_frames(ctx):
     """Overlapping windows submitted with frame keys: frames upload once and are shared."""
     rng = np.random.default_rng(1)
