@@ -814,12 +814,17 @@ def run_shake(args):
 
 
 def run_ingest(args):
-    """Frame ingest: the HD stack written as 64 PNG files (Paeth-filtered, zlib level 6),
-    decoded by cp_load_png on all host threads into pinned memory, then composited from there
-    by cp_composite (abs/0.05/0.2 average): files -> composite, the work the reference does
-    per frame inside its slicing loop (src/streams.rs:63-70), and the composite and blend
-    mask written back as PNG files by cp_save_png (src/main.rs:519-570): files -> files.
-    Also reports one-thread decode, the reference's per-frame sequential decode rate."""
+    """Frame ingest: the HD stack (64 x 1920x1080 RGB) as files -> composite, the work the
+    reference does per frame inside its slicing loop (src/streams.rs:63-70).
+
+    value: JPEG frames/s. The frames written as baseline JPEG at quality 95 (the quality of
+    the reference's example frames, src/util/create_example_data.rs:56), read on host
+    threads and decoded by nvJPEG (the GPU's JPEG engines) straight into device memory by
+    cp_load_jpeg_device. Also: files -> composite (decode, then cp_composite_device,
+    abs/0.05/0.2 average, and the composite and blend mask copied back), files -> files (the
+    composite and mask written as JPEG by cp_save_jpeg, src/main.rs:542-556), the decode to
+    host memory (cp_load_jpeg), and the same with PNG files (cp_load_png on all host
+    threads, then cp_composite from pinned memory; outputs by cp_save_png)."""
     import shutil
     import tempfile
     import numpy as np
@@ -828,49 +833,106 @@ def run_ingest(args):
     fb = W * H * C
     frames = example_data.hd_stack(seed=2)
     tmp = tempfile.mkdtemp(prefix="cp_ingest_")
+    steps = max(1, min(args.steps, 5))
+    threads = os.cpu_count() or 1
+    keep = []
+    p = make_params(keep=keep, mode="outlier", threshold="abs/0.05/0.2", outlier="average",
+                    background="first")
     try:
-        threads = os.cpu_count() or 1
-        paths = example_data.write_pngs(frames, tmp, level=6, threads=threads)
-        file_bytes = sum(os.path.getsize(p) for p in paths)
+        # ---- JPEG ---------------------------------------------------------------------------
+        t0 = time.perf_counter()
+        jpaths = []
+        for i in range(N_FRAMES):
+            jp = os.path.join(tmp, "image-%05d.jpg" % i)
+            ctx.check(lib.cp_save_jpeg(ctx.handle, jp.encode(), frames[i].ctypes.data, W, H, C,
+                                       95, 0, 0), "cp_save_jpeg")
+            jpaths.append(jp)
+        t_jenc_frames = time.perf_counter() - t0
+        jbytes = sum(os.path.getsize(q) for q in jpaths)
+        jarr = (ct.c_char_p * N_FRAMES)(*[q.encode() for q in jpaths])
+        stride = (fb + 15) // 16 * 16
+        dev = ctx.alloc(N_FRAMES * stride + 16)
+        out_d, blend_d = ctx.alloc(fb), ctx.alloc(fb)
+        optr, _ = _pinned(ctx, lib, 2 * fb)
+        stack = _abi.Stack(n=N_FRAMES, width=W, height=H, channels=C, base=dev,
+                           frame_stride=stride)
+
+        def jdecode():
+            ctx.check(lib.cp_load_jpeg_device(ctx.handle, jarr, N_FRAMES, threads, dev, stride,
+                                              W, H, C), "cp_load_jpeg_device")
+
+        def jcomposite():
+            ctx.check(lib.cp_composite_device(ctx.handle, ct.byref(stack), ct.byref(p), out_d,
+                                              blend_d, None, None, None), "cp_composite_device")
+            ctx.check(lib.cp_memcpy_d2h(ctx.handle, optr, out_d, fb, None), "d2h")
+            ctx.check(lib.cp_memcpy_d2h(ctx.handle, optr + fb, blend_d, fb, None), "d2h")
+
+        jdecode()
+        jcomposite()
+        # decoded frames against the sources (JPEG is lossy: the quantisation error)
+        raw = ctx.download(dev, (stride,))[:fb].reshape(H, W, C)
+        jerr = np.abs(raw.astype(np.int16) - frames[0].astype(np.int16))
+        t_dec = t_comp = 0.0
+        with ClockSampler(local) as clk:
+            for _ in range(steps):
+                t0 = time.perf_counter()
+                jdecode()
+                t1 = time.perf_counter()
+                jcomposite()
+                t2 = time.perf_counter()
+                t_dec += t1 - t0
+                t_comp += t2 - t1
+        t_dec /= steps
+        t_comp /= steps
+        t0 = time.perf_counter()
+        for k, name in enumerate(("composite.jpg", "blend.jpg")):
+            ctx.check(lib.cp_save_jpeg(ctx.handle, os.path.join(tmp, name).encode(),
+                                       optr + k * fb, W, H, C, 95, 0, 0), "cp_save_jpeg")
+        t_jenc = time.perf_counter() - t0
         hptr, host = _pinned(ctx, lib, N_FRAMES * fb)
+        ctx.check(lib.cp_load_jpeg(ctx.handle, jarr, N_FRAMES, threads, hptr, fb, W, H, C))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.check(lib.cp_load_jpeg(ctx.handle, jarr, N_FRAMES, threads, hptr, fb, W, H, C),
+                      "cp_load_jpeg")
+        t_jhost = (time.perf_counter() - t0) / steps
+        for q in (dev, out_d, blend_d):
+            ctx.free(q)
+
+        # ---- PNG ----------------------------------------------------------------------------
+        paths = example_data.write_pngs(frames, tmp, level=6, threads=threads)
+        file_bytes = sum(os.path.getsize(q) for q in paths)
         host = host.reshape(N_FRAMES, H, W, C)
-        arr = (ct.c_char_p * N_FRAMES)(*[p.encode() for p in paths])
+        arr = (ct.c_char_p * N_FRAMES)(*[q.encode() for q in paths])
 
         def decode(nthreads, n=N_FRAMES):
             ctx.check(lib.cp_load_png(ctx.handle, arr, n, nthreads, hptr, fb, W, H, C),
                       "cp_load_png")
         decode(threads)
         exact = bool(np.array_equal(host, frames))
-        keep = []
-        p = make_params(keep=keep, mode="outlier", threshold="abs/0.05/0.2", outlier="average",
-                        background="first")
-        stack = _abi.Stack(n=N_FRAMES, width=W, height=H, channels=C, base=hptr,
-                           frame_stride=fb)
-        optr, _ = _pinned(ctx, lib, 2 * fb)
+        hstack = _abi.Stack(n=N_FRAMES, width=W, height=H, channels=C, base=hptr,
+                            frame_stride=fb)
 
         def composite():
-            ctx.check(lib.cp_composite(ctx.handle, ct.byref(stack), ct.byref(p), optr,
+            ctx.check(lib.cp_composite(ctx.handle, ct.byref(hstack), ct.byref(p), optr,
                                        optr + fb, None, None), "cp_composite")
         composite()
-        steps = max(1, min(args.steps, 5))
-        t_dec = t_comp = 0.0
-        with ClockSampler(local) as clk:
-            for _ in range(steps):
-                t0 = time.perf_counter()
-                decode(threads)
-                t1 = time.perf_counter()
-                composite()
-                t2 = time.perf_counter()
-                t_dec += t1 - t0
-                t_comp += t2 - t1
-        t_dec /= steps
-        t_comp /= steps
+        p_dec = p_comp = 0.0
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            decode(threads)
+            t1 = time.perf_counter()
+            composite()
+            t2 = time.perf_counter()
+            p_dec += t1 - t0
+            p_comp += t2 - t1
+        p_dec /= steps
+        p_comp /= steps
         n1 = 8
         decode(1, n1)
         t0 = time.perf_counter()
         decode(1, n1)
         t_one = (time.perf_counter() - t0) / n1
-        # output encode: the composite and its blend mask as PNG files (zlib level 6)
         t0 = time.perf_counter()
         for k, name in enumerate(("composite.png", "blend.png")):
             ctx.check(lib.cp_save_png(ctx.handle, os.path.join(tmp, name).encode(),
@@ -880,22 +942,43 @@ def run_ingest(args):
         shutil.rmtree(tmp, ignore_errors=True)
     print(json.dumps({
         "workload": "ingest", "metric": "frames/s", "value": N_FRAMES / t_dec, "unit": "frames/s",
-        "threads": threads, "decoded_exact": exact,
+        "format": "jpeg", "threads": threads,
         "decode_ms_per_stack": 1e3 * t_dec, "decoded_MB_per_s": N_FRAMES * fb / t_dec / 1e6,
-        "one_thread_frames_per_s": 1.0 / t_one,
+        "decoder": "nvJPEG batched decode (JPEG engines), file reads on host threads, frames "
+                   "written to device memory",
+        "decode_error_vs_source": {"max": int(jerr.max()), "mean": float(jerr.mean()),
+                                   "note": "frame 0; the JPEG quantisation error at quality 95"},
         "files_to_composite": {"value": MPXF_PER_COMPOSITE / (t_dec + t_comp), "unit": METRIC,
-                               "decode_ms": 1e3 * t_dec, "composite_e2e_ms": 1e3 * t_comp,
-                               "note": "decode, then cp_composite from pinned memory (H2D, "
-                                       "kernel, D2H of composite and mask)"},
-        "encode_ms": 1e3 * t_enc,
-        "files_to_files": {"value": MPXF_PER_COMPOSITE / (t_dec + t_comp + t_enc),
+                               "decode_ms": 1e3 * t_dec, "composite_ms": 1e3 * t_comp,
+                               "note": "cp_load_jpeg_device, then cp_composite_device and the "
+                                       "composite and mask copied to pinned memory"},
+        "encode_ms": 1e3 * t_jenc,
+        "files_to_files": {"value": MPXF_PER_COMPOSITE / (t_dec + t_comp + t_jenc),
                            "unit": METRIC,
-                           "note": "the above plus cp_save_png of composite and mask "
-                                   "(each on all host threads), in sequence"},
-        "steps": steps, "dtype": "u8", "data": "synthetic (seeded HD stack written as PNG)",
+                           "note": "the above plus cp_save_jpeg of composite and mask at "
+                                   "quality 95 (each on all host threads), in sequence"},
+        "decode_to_host": {"value": N_FRAMES / t_jhost, "unit": "frames/s",
+                           "note": "cp_load_jpeg: decoded on the device, copied to pinned "
+                                   "host memory"},
+        "frame_encode_ms": 1e3 * t_jenc_frames / N_FRAMES,
+        "png": {"value": N_FRAMES / p_dec, "unit": "frames/s", "decoded_exact": exact,
+                "decode_ms_per_stack": 1e3 * p_dec,
+                "one_thread_frames_per_s": 1.0 / t_one,
+                "files_to_composite": {"value": MPXF_PER_COMPOSITE / (p_dec + p_comp),
+                                       "unit": METRIC, "decode_ms": 1e3 * p_dec,
+                                       "composite_e2e_ms": 1e3 * p_comp},
+                "encode_ms": 1e3 * t_enc,
+                "files_to_files": {"value": MPXF_PER_COMPOSITE / (p_dec + p_comp + t_enc),
+                                   "unit": METRIC},
+                "note": "cp_load_png on all host threads into pinned memory, then cp_composite "
+                        "(H2D, kernel, D2H); outputs by cp_save_png",
+                "config": {"png": "8-bit RGB, Paeth filter, zlib level 6",
+                           "compressed_MB_per_frame": file_bytes / N_FRAMES / 1e6}},
+        "steps": steps, "dtype": "u8", "data": "synthetic (seeded HD stack written as JPEG "
+                                               "and PNG)",
         "config": {"frames": N_FRAMES, "width": W, "height": H, "channels": C,
-                   "png": "8-bit RGB, Paeth filter, zlib level 6",
-                   "compressed_MB_per_frame": file_bytes / N_FRAMES / 1e6},
+                   "jpeg": "baseline, 4:4:4, quality 95, restart interval of one MCU row",
+                   "compressed_MB_per_frame": jbytes / N_FRAMES / 1e6},
         "clocks": clk.summary()}), flush=True)
 
 

@@ -6,5 +6,6 @@ the reference's processor interface in Python (api.py).
 """
 from ._abi import ChronoError, lib  # noqa: F401
 from .api import (Context, Crop, Fade, OutlierProcessor, Server, ShakeAnalyzer,  # noqa: F401
-                  SimpleProcessor, Threshold, default_context, load_png, make_params,
-                  png_info, save_png, video_windows)
+                  SimpleProcessor, Threshold, default_context, encode_jpeg, jpeg_info,
+                  load_jpeg, load_png, make_params, png_info, save_image, save_jpeg, save_png,
+                  video_windows)

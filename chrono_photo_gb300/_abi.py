@@ -123,6 +123,13 @@ SIGNATURES = [
     ("cp_png_info", ct.c_int, [P, ct.c_char_p, I32P, I32P, I32P]),
     ("cp_load_png", ct.c_int, [P, ct.POINTER(ct.c_char_p), I32, I32, P, U64, I32, I32, I32]),
     ("cp_save_png", ct.c_int, [P, ct.c_char_p, P, I32, I32, I32, I32, I32]),
+    ("cp_jpeg_info", ct.c_int, [P, ct.c_char_p, I32P, I32P, I32P]),
+    ("cp_load_jpeg", ct.c_int, [P, ct.POINTER(ct.c_char_p), I32, I32, P, U64, I32, I32, I32]),
+    ("cp_load_jpeg_device", ct.c_int, [P, ct.POINTER(ct.c_char_p), I32, I32, P, U64, I32, I32,
+                                       I32]),
+    ("cp_save_jpeg", ct.c_int, [P, ct.c_char_p, P, I32, I32, I32, I32, I32, I32]),
+    ("cp_encode_jpeg", ct.c_int, [P, P, I32, I32, I32, I32, I32, I32, P, U64,
+                                  ct.POINTER(ct.c_uint64)]),
 ]
 
 _lib = None

@@ -10,8 +10,9 @@
 
 Frames are numpy uint8 arrays [n, height, width, channels] (or a list of [h, w, c] arrays):
 the decoded images the reference reads through `image::open`; the processors also take a
-list of PNG file paths, as the reference's take files (decoded by cp_load_png). Every
-composite runs on the GPU; there is no CPU path.
+list of PNG or JPEG file paths, as the reference's take files (PNG decoded by cp_load_png on
+host threads, JPEG by nvJPEG on the GPU straight into device frames). Every composite runs on
+the GPU; there is no CPU path.
 """
 import ctypes as ct
 import os
@@ -140,11 +141,22 @@ def _is_paths(frames):
         all(isinstance(f, (str, os.PathLike)) for f in frames)
 
 
+_JPEG_EXT = (".jpg", ".jpeg", ".jpe", ".jfif")
+
+
+def _is_jpeg(path):
+    return str(path).lower().endswith(_JPEG_EXT)
+
+
 def _as_stack(frames):
-    """uint8 [n, h, w, c] from an array, a sequence of images, or a sequence of PNG file
-    paths (decoded by cp_load_png on all host threads, as the reference's processors take
-    their frames as files)."""
+    """uint8 [n, h, w, c] from an array, a sequence of images, or a sequence of PNG or JPEG
+    file paths (PNG decoded by cp_load_png on all host threads, JPEG by cp_load_jpeg on the
+    GPU, as the reference's processors take their frames as files)."""
     if _is_paths(frames):
+        if all(_is_jpeg(f) for f in frames):
+            return load_jpeg(frames)
+        if any(_is_jpeg(f) for f in frames):
+            raise ValueError("a stack of files is all JPEG or all PNG")
         return load_png(frames)
     if isinstance(frames, np.ndarray):
         a = np.ascontiguousarray(frames, dtype=np.uint8)
@@ -155,13 +167,14 @@ def _as_stack(frames):
 
 
 def _select(frames, image_indices):
-    """The stack of the frames at image_indices (all when None) and its frame offset
-    (src/chrono.rs:103): paths are selected before decoding."""
+    """The frames at image_indices (all when None) and their frame offset
+    (src/chrono.rs:103). File paths stay paths (selected before decoding, and decoded by
+    Context.composite: JPEG straight into device memory); anything else becomes a stack."""
     if image_indices is None:
-        return _as_stack(frames), 0
+        return (list(frames) if _is_paths(frames) else _as_stack(frames)), 0
     idx = [int(i) for i in image_indices]
     if _is_paths(frames):
-        return _as_stack([frames[i] for i in idx]), idx[0]
+        return [frames[i] for i in idx], idx[0]
     return np.ascontiguousarray(_as_stack(frames)[idx]), idx[0]
 
 
@@ -225,6 +238,9 @@ class Context:
         (composite, blend_mask or None, warnings[, debug dict])."""
         keep = []
         p = params if params is not None else make_params(keep=keep, **kw)
+        if (_is_paths(frames) and all(_is_jpeg(f) for f in frames) and not debug
+                and crop is None):
+            return self._composite_jpeg(frames, p, blend, frame_offset)
         a = _as_stack(frames)
         n, h, w, c = a.shape
         st = _abi.Stack()
@@ -270,6 +286,57 @@ class Context:
         if debug:
             return out, bl, warn.value, dbg_arrays
         return out, bl, warn.value
+
+    def load_jpeg_device(self, paths, threads=0):
+        """Decodes JPEG files on the GPU (cp_load_jpeg_device) into one new device buffer:
+        returns (pointer, frame_stride, (n, h, w, c)); frames start on 16-byte boundaries
+        with 16 spare bytes after the last, as the compositing kernels read them. Free the
+        buffer with free()."""
+        paths = [str(f) for f in paths]
+        if not paths:
+            raise ValueError("no frames")
+        w, h, c = jpeg_info(paths[0])
+        fb = w * h * c
+        stride = (fb + 15) // 16 * 16
+        dev = self.alloc(len(paths) * stride + 16)
+        try:
+            arr = (ct.c_char_p * len(paths))(*[f.encode() for f in paths])
+            self.check(lib().cp_load_jpeg_device(self.handle, arr, len(paths), int(threads), dev,
+                                                 stride, w, h, c), "cp_load_jpeg_device")
+        except Exception:
+            self.free(dev)
+            raise
+        return dev, stride, (len(paths), h, w, c)
+
+    def _composite_jpeg(self, paths, p, blend, frame_offset):
+        """JPEG files -> composite with the frames decoded into device memory (only the
+        compressed bytes cross the host link), then cp_composite_device and the results
+        copied back."""
+        dev, stride, (n, h, w, c) = self.load_jpeg_device(paths)
+        ptrs = [dev]
+        try:
+            fb = h * w * c
+            out_d = self.alloc(fb)
+            ptrs.append(out_d)
+            bl_d = None
+            if blend and p.mode == 0:
+                bl_d = self.alloc(fb)
+                ptrs.append(bl_d)
+            warn_d = self.upload(np.zeros(1, np.uint64))
+            ptrs.append(warn_d)
+            st = _abi.Stack(n=n, width=w, height=h, channels=c, base=dev, frame_stride=stride,
+                            frame_offset=frame_offset)
+            self.check(lib().cp_composite_device(self.handle, ct.byref(st), ct.byref(p), out_d,
+                                                 bl_d, None, warn_d, None),
+                       "cp_composite_device")
+            self.synchronize()
+            out = self.download(out_d, (h, w, c))
+            bl = self.download(bl_d, (h, w, c)) if bl_d is not None else None
+            warn = int(self.download(warn_d, (1,), np.uint64)[0])
+            return out, bl, warn
+        finally:
+            for q in ptrs:
+                self.free(q)
 
     def composite_multi(self, frames, params_list, blend=True):
         """One host-memory stack under several parameter sets (cp_composite_multi): the
@@ -421,6 +488,81 @@ def save_png(path, image, level=6, threads=0, context=None):
     handle = context.handle if context else None
     _check(handle, lib().cp_save_png(handle, str(path).encode(), a.ctypes.data, w, h, c,
                                      int(level), int(threads)), "cp_save_png")
+
+
+def jpeg_info(path):
+    """(width, height, channels) of a JPEG file (cp_jpeg_info): channels 1 (gray) or 3."""
+    w, h, c = ct.c_int32(), ct.c_int32(), ct.c_int32()
+    _check(None, lib().cp_jpeg_info(None, str(path).encode(), ct.byref(w), ct.byref(h),
+                                    ct.byref(c)), "cp_jpeg_info")
+    return w.value, h.value, c.value
+
+
+def load_jpeg(paths, threads=0, out=None, context=None):
+    """Decodes JPEG frames on the GPU (cp_load_jpeg, nvJPEG) into host uint8 [n, h, w, c]
+    (c = 3 for colour, 1 for gray), the replacement of the reference's per-frame
+    `image::open` (src/streams.rs:63-70). `out`: optional C-contiguous destination of that
+    shape (e.g. pinned memory). Context.load_jpeg_device keeps the frames on the device."""
+    paths = [str(p) for p in paths]
+    if not paths:
+        raise ValueError("no frames")
+    ctx = context or default_context()
+    w, h, c = jpeg_info(paths[0])
+    if out is None:
+        out = np.empty((len(paths), h, w, c), np.uint8)
+    if out.shape != (len(paths), h, w, c) or out.dtype != np.uint8 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous uint8 array of shape %s"
+                         % ((len(paths), h, w, c),))
+    arr = (ct.c_char_p * len(paths))(*[p.encode() for p in paths])
+    ctx.check(lib().cp_load_jpeg(ctx.handle, arr, len(paths), int(threads), out.ctypes.data,
+                                 h * w * c, w, h, c), "cp_load_jpeg")
+    return out
+
+
+_SUBSAMPLING = {"444": 0, "4:4:4": 0, "420": 1, "4:2:0": 1}
+
+
+def encode_jpeg(image, quality=95, subsampling="444", threads=0, context=None):
+    """The baseline JPEG bytes of a uint8 [h, w, c] image (cp_encode_jpeg; c = 1, 3 or 4,
+    the alpha of 4 dropped), quality 1..100, chroma subsampling "444" (the reference's
+    encoder) or "420"."""
+    a = np.ascontiguousarray(image, dtype=np.uint8)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    h, w, c = a.shape
+    handle = context.handle if context else None
+    size = ct.c_uint64(0)
+    cap = 1024 + 2 * a.nbytes
+    buf = np.empty(cap, np.uint8)
+    _check(handle, lib().cp_encode_jpeg(handle, a.ctypes.data, w, h, c, int(quality),
+                                        _SUBSAMPLING[subsampling], int(threads),
+                                        buf.ctypes.data, cap, ct.byref(size)), "cp_encode_jpeg")
+    return buf[:size.value].tobytes()
+
+
+def save_jpeg(path, image, quality=95, subsampling="444", threads=0, context=None):
+    """Writes a uint8 [h, w, c] image as a baseline JPEG file (cp_save_jpeg), creating a
+    missing parent directory: the .jpg branch of the reference's save_image
+    (src/main.rs:542-556), quality 95 by default as its --quality."""
+    a = np.ascontiguousarray(image, dtype=np.uint8)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    h, w, c = a.shape
+    handle = context.handle if context else None
+    _check(handle, lib().cp_save_jpeg(handle, str(path).encode(), a.ctypes.data, w, h, c,
+                                      int(quality), _SUBSAMPLING[subsampling], int(threads)),
+           "cp_save_jpeg")
+
+
+def save_image(path, image, quality=95, threads=0, context=None):
+    """save_image of src/main.rs:519-570: JPEG for a .jpg / .jpeg extension (at `quality`),
+    PNG otherwise; a missing parent directory is created."""
+    if _is_jpeg(path):
+        save_jpeg(path, image, quality=quality, threads=threads, context=context)
+    elif str(path).lower().endswith(".png"):
+        save_png(path, image, threads=threads, context=context)
+    else:
+        raise ValueError("output format by extension: .png, .jpg or .jpeg")
 
 
 def video_windows(image_count, video_in, video_out=(None, None, 1)):

@@ -651,6 +651,7 @@ void cp_ctx_destroy(cp_ctx* ctx) {
   cudaStreamSynchronize(ctx->copy_stream2);
   cudaStreamSynchronize(ctx->d2h_stream);
   release_plans(ctx);
+  jpeg_release(ctx);
   std::vector<void*> ptrs;
   for (auto& kv : ctx->allocs) ptrs.push_back(kv.first);
   for (void* q : ptrs) cudaFree(q);

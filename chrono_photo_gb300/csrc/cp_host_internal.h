@@ -79,6 +79,7 @@ struct cp_ctx {
   std::vector<cudaEvent_t> band_events;
   // batch plans (graph-captured persistent launches)
   std::vector<std::unique_ptr<cp::BatchPlan>> plans;
+  void* jpeg = nullptr;  // the JPEG decoder (cp_jpeg.cpp), created at the first JPEG call
 };
 
 namespace cp {
@@ -102,6 +103,7 @@ int ensure_buffer(cp_ctx* ctx, DevBuffer& b, uint64_t bytes);
 int ensure_pinned(cp_ctx* ctx, PinnedBuffer& b, uint64_t bytes);
 bool is_pinned(const void* p);
 void release_plans(cp_ctx* ctx);
+void jpeg_release(cp_ctx* ctx);  // frees the context's JPEG decoder, if any
 // Batched launches (cp_batch.cpp): the specialised batched kernel a stack takes (index in
 // CP_BATCH_VARIANTS, -1: the general kernel), and one launch over device descriptors.
 int batch_variant_key(const StackDev& d);

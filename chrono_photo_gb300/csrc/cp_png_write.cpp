@@ -25,9 +25,13 @@
 
 #include "../../include/chrono_gpu.h"
 #include "cp_host_internal.h"
+#include "cp_io.h"
 #include "cp_png.h"
 
 namespace {
+
+using cp::open_output;
+using cp::run_parallel;
 
 constexpr int kWindow = 32768;
 constexpr int kMinMatch = 3, kMaxMatch = 258;
@@ -432,36 +436,6 @@ void write_block(BitWriter& bw, const std::vector<Token>* tok_list, const uint8_
   bw.put(lcode[256], L[256]);
 }
 
-// Runs fn(0) .. fn(count - 1) on up to `threads` threads (0: all cores), each index once.
-// An exception in fn stops the remaining work and is rethrown (as std::bad_alloc) on the
-// calling thread after every worker has joined; if fewer threads start than asked for, the
-// started ones share the work.
-template <typename Fn>
-void run_parallel(size_t count, int threads, Fn fn) {
-  int workers = threads > 0 ? threads : static_cast<int>(std::thread::hardware_concurrency());
-  workers = std::max(1, std::min<int>(workers, static_cast<int>(std::min<size_t>(count, 1024))));
-  std::atomic<size_t> next(0);
-  std::atomic<bool> failed(false);
-  auto work = [&]() {
-    for (size_t i = next.fetch_add(1); i < count && !failed.load(); i = next.fetch_add(1)) {
-      try {
-        fn(i);
-      } catch (const std::exception&) {
-        failed.store(true);
-      }
-    }
-  };
-  std::vector<std::thread> pool;
-  try {
-    pool.reserve(static_cast<size_t>(workers));
-    for (int t = 1; t < workers; ++t) pool.emplace_back(work);
-  } catch (const std::exception&) {
-  }
-  work();
-  for (auto& t : pool) t.join();
-  if (failed.load()) throw std::bad_alloc();
-}
-
 // Compressed independently: the filtered data is cut into segments of this many bytes, a
 // fixed size so that the file does not depend on the number of threads.
 constexpr size_t kSegment = 256 * 1024;
@@ -604,21 +578,6 @@ void put_chunk(std::vector<uint8_t>* png, const char* type, const uint8_t* body,
   uint8_t tail[4];
   cp::png::put_be32(tail, crc);
   png->insert(png->end(), tail, tail + 4);
-}
-
-// Opens `path` for writing; when its parent directory is missing, creates it (one level, as
-// std::fs::create_dir in the reference) and tries again.
-FILE* open_output(const char* path) {
-  FILE* f = std::fopen(path, "wb");
-  if (f) return f;
-  std::string dir(path);
-  const size_t slash = dir.find_last_of('/');
-  if (slash == std::string::npos || slash == 0) return nullptr;
-  dir.resize(slash);
-  struct stat st;
-  if (stat(dir.c_str(), &st) == 0) return nullptr;  // the parent exists: a real error
-  if (mkdir(dir.c_str(), 0777) != 0) return nullptr;
-  return std::fopen(path, "wb");
 }
 
 // The body of cp_save_png (which keeps C++ exceptions from crossing the C ABI).

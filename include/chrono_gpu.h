@@ -44,7 +44,7 @@ extern "C" {
 #define CP_ERR_STATE (-7)   /* object in the wrong state (stopped server, unknown job)     */
 #define CP_ERR_NODEV (-8)   /* no CUDA device with compute capability 10.3                 */
 #define CP_ERR_LIMIT (-9)   /* request above a fixed limit (batch_static, composite_multi) */
-#define CP_ERR_IO (-10)     /* image file missing, unreadable or not a supported PNG       */
+#define CP_ERR_IO (-10)     /* image file missing, unreadable or not a supported PNG/JPEG  */
 #define CP_ERR_CANCELLED (-11) /* server job cancelled before it started                   */
 
 /* ---- option enums (src/options.rs) --------------------------------------------------- */
@@ -306,6 +306,28 @@ int cp_load_png(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t thread
                 uint8_t* out, uint64_t frame_stride, int32_t width, int32_t height,
                 int32_t channels);
 
+/* The same for JPEG files (the reference's own frames are JPEG: image-%05d.jpg at quality
+ * 95, src/util/create_example_data.rs:52-56), decoded on the GPU by nvJPEG's batched
+ * decoder (libnvjpeg, loaded at the first call): Huffman-coded DCT, baseline, extended or
+ * progressive, 8-bit samples, one component (channels 1, gray) or three (channels 3,
+ * interleaved RGB); any chroma subsampling nvJPEG takes. Files are read on `threads` host
+ * threads (0: all cores) and their headers checked against width, height and channels.
+ * cp_load_jpeg_device writes frame i to out + i * frame_stride in DEVICE memory (the stack
+ * of cp_composite_device: only the compressed bytes cross the host link); cp_load_jpeg to
+ * host memory (decoded on the device, then copied back). Both return when the frames are
+ * written. JPEG decoders differ in their inverse DCT and chroma upsampling, so the samples
+ * match those of image's decoder to a tolerance, not bit for bit. CP_ERR_IO for a missing,
+ * truncated, corrupt or unsupported file (lossless, hierarchical, arithmetic-coded, 12-bit,
+ * CMYK) or when libnvjpeg cannot be loaded. cp_jpeg_info reads a file's header (host only). */
+int cp_jpeg_info(cp_ctx* ctx, const char* path, int32_t* width, int32_t* height,
+                 int32_t* channels);
+int cp_load_jpeg_device(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t threads,
+                        uint8_t* out, uint64_t frame_stride, int32_t width, int32_t height,
+                        int32_t channels);
+int cp_load_jpeg(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t threads,
+                 uint8_t* out, uint64_t frame_stride, int32_t width, int32_t height,
+                 int32_t channels);
+
 /* ---- output encode ----------------------------------------------------------------------- */
 /* Replaces save_image (src/main.rs:519-570: image::save_buffer by file extension, the parent
  * directory created when missing) for PNG output of a composite or blend mask: `image` is
@@ -315,6 +337,23 @@ int cp_load_png(cp_ctx* ctx, const char* const* paths, int32_t n, int32_t thread
  * ctx (nullable) receives the error message; CP_ERR_IO when the file cannot be written. */
 int cp_save_png(cp_ctx* ctx, const char* path, const uint8_t* image, int32_t width,
                 int32_t height, int32_t channels, int32_t level, int32_t threads);
+
+/* Replaces the .jpg branch of save_image (src/main.rs:542-556: image's JPEGEncoder at
+ * --quality, 95 by default, src/cli.rs:82-84): baseline JPEG of a host image (channels 1
+ * gray, 3 RGB, 4 RGBA with the alpha dropped, as image does), quality 1..100 (0 or less:
+ * 95) with the IJG scaling of the Annex K tables, chroma `subsampling` 0 = 4:4:4 (the
+ * reference's) or 1 = 4:2:0, Huffman tables built for the image, one restart interval per
+ * MCU row so that rows are coded on `threads` host threads (0: all cores; the file does not
+ * depend on it). Width and height up to 65535. cp_save_jpeg writes the file (creating a
+ * missing parent directory); cp_encode_jpeg writes the bytes to out[0, capacity) and their
+ * count to *size (CP_ERR_LIMIT, with *size set, when they do not fit; capacity 0 queries
+ * the size). */
+int cp_save_jpeg(cp_ctx* ctx, const char* path, const uint8_t* image, int32_t width,
+                 int32_t height, int32_t channels, int32_t quality, int32_t subsampling,
+                 int32_t threads);
+int cp_encode_jpeg(cp_ctx* ctx, const uint8_t* image, int32_t width, int32_t height,
+                   int32_t channels, int32_t quality, int32_t subsampling, int32_t threads,
+                   uint8_t* out, uint64_t capacity, uint64_t* size);
 
 /* ---- serving ------------------------------------------------------------------------- */
 /* A compositing job: a host-memory stack plus options, output buffers in host memory.

@@ -104,7 +104,7 @@ def _addr(s):
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
-SRC = os.path.join(HERE, "chrono_oracle.cpp")
+SRCS = [os.path.join(HERE, "chrono_oracle.cpp"), os.path.join(HERE, "jpeg_oracle.cpp")]
 
 _lib = None
 
@@ -112,10 +112,10 @@ _lib = None
 def build():
     """Compile liboracle.so with -ffp-contract=off (f32 ops rounded one by one, like rustc)."""
     hdr = os.path.join(HERE, "..", "include", "chrono_gpu.h")
-    if (not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC)
-            or os.path.getmtime(LIB) < os.path.getmtime(hdr)):
+    if (not os.path.exists(LIB)
+            or any(os.path.getmtime(LIB) < os.path.getmtime(f) for f in SRCS + [hdr])):
         cmd = [os.environ.get("CXX", "g++"), "-O3", "-std=c++17", "-fPIC", "-pthread",
-               "-ffp-contract=off", "-fno-fast-math", "-shared", "-o", LIB + ".tmp", SRC]
+               "-ffp-contract=off", "-fno-fast-math", "-shared", "-o", LIB + ".tmp"] + SRCS
         subprocess.run(cmd, check=True, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -129,6 +129,9 @@ def lib():
         P = ct.c_void_p
         l.or_quartiles.argtypes = [P, ct.c_int32, ct.POINTER(ct.c_float), ct.POINTER(ct.c_float),
                                    ct.POINTER(ct.c_float)]
+        l.or_jpeg_info.argtypes = [P, ct.c_size_t, ct.POINTER(ct.c_int32),
+                                   ct.POINTER(ct.c_int32), ct.POINTER(ct.c_int32)]
+        l.or_jpeg_decode.argtypes = [P, ct.c_size_t, P, ct.c_size_t]
         l.or_median.argtypes = [P, ct.c_int32]
         l.or_median.restype = ct.c_float
         l.or_blend_value.argtypes = [ct.c_int32, ct.c_float, ct.c_float, ct.c_float]
@@ -245,3 +248,17 @@ def video_windows(image_count, video_in, video_out=(None, None, 1)):
                            idx.ctypes.data, frames.ctypes.data)
     return [(int(frames[i]), [int(v) for v in idx[starts[i]:starts[i] + lens[i]]])
             for i in range(nw.value)]
+
+
+def jpeg_decode(data):
+    """A sequential (baseline or extended) JPEG file's bytes decoded by the exact-IDCT
+    reference decoder (jpeg_oracle.cpp): uint8 [h, w, c], c = 1 or 3."""
+    buf = np.frombuffer(bytes(data), np.uint8)
+    w, h, c = ct.c_int32(), ct.c_int32(), ct.c_int32()
+    l = lib()
+    if l.or_jpeg_info(buf.ctypes.data, buf.size, ct.byref(w), ct.byref(h), ct.byref(c)) != 0:
+        raise ValueError("not a sequential 8-bit JPEG the oracle reads")
+    out = np.empty((h.value, w.value, c.value), np.uint8)
+    if l.or_jpeg_decode(buf.ctypes.data, buf.size, out.ctypes.data, out.nbytes) != 0:
+        raise ValueError("corrupt JPEG data")
+    return out
