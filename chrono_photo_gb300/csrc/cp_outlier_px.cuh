@@ -24,15 +24,18 @@
 namespace cp {
 namespace {
 
-template <int NW, bool DB>
-constexpr int kPxMinCtas = NW == 1 ? 6 : (NW == 2 ? (DB ? 4 : 5) : 2);
+// CTAs per SM the register allocation is made for. Per-pixel phase A (PA 2) fits 72
+// registers without spills at two plane words, so 7 CTAs (the shared-memory limit of a
+// 64-frame tile) are resident; the word-column layout needs 96 (5 CTAs).
+template <int NW, bool DB, int PA>
+constexpr int kPxMinCtas = NW == 1 ? 6 : (NW == 2 ? (DB ? 4 : (PA == 2 ? 7 : 5)) : 2);
 
 // PA: how phase A runs. 0: warps 0..2, word per lane, 4 byte positions per selection round;
 // 1: the same with 2 byte positions per round (fewer registers); 2: every warp builds the
 // planes of its own pixel's samples (no exchange, no idle warp, a quarter of each transpose
 // unused).
 template <int KIND, int OG, int BG, int NW, bool DB, int PA = 0>
-__global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB>))
+__global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB, PA>))
     k_outlier_px(const __grid_constant__ StackDev S, uint32_t* error) {
   constexpr int C = 3;
   extern __shared__ __align__(128) uint8_t smem[];
@@ -184,12 +187,12 @@ __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB>))
   flush_warnings(S.warnings, warn);
 }
 
-// Static phase-A choice per kind (what the autotuner starts from), as measured on the
-// 64 x 1080p stack: word-column selection for integer (abs) distances (0.293 ms vs 0.300
-// per-pixel), per-pixel planes for rel thresholds, whose six selections per channel spill in
-// the word-column layout (0.482 vs 0.517 ms).
+// Static phase-A choice (what the autotuner starts from): per-pixel planes for every kind.
+// Measured on the 64 x 1080p stack with 7 CTAs per SM against the word-column layout's 5:
+// abs average 0.278 vs 0.288 ms, rel average 0.451 vs 0.496 ms (whose six selections per
+// channel spill in the word-column layout).
 template <int KIND>
-constexpr int kPxPhaseA = KIND == kF32Kind ? 2 : 0;
+constexpr int kPxPhaseA = 2;
 
 template <int KIND, int OG, int BG, int NW, bool DB, int PA>
 int px_launch_t(const StackDev& s, int grid, int smem, void* stream, uint32_t* error) {

@@ -175,7 +175,7 @@ PxChoice tune(cp_ctx* ctx, int k, int g, int b, const StackDev& d, cudaStream_t 
   cudaEventCreate(&e1);
   PxChoice best;
   best.ms = 1e30f;
-  const int static_pa = k == 2 ? 2 : 0;
+  const int static_pa = 2;  // kPxPhaseA
   float static_ms = 0.0f;
   for (int pa : {0, 2}) {
     for (int db = 0; db < 2; ++db) {
@@ -268,7 +268,7 @@ int launch_px(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
       }
     }
   }
-  if (c.pa < 0) c.pa = k == 2 ? 2 : 0;
+  if (c.pa < 0) c.pa = 2;  // kPxPhaseA
   return px_run(ctx, k, g, b, d, c, stream);
 }
 
