@@ -215,7 +215,7 @@ def measured_peaks():
 def profiled(key):
     """A per-launch figure (`dram_bytes_per_launch`, `warp_instructions_per_launch`) of the
     abs/average outlier launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_composite_outlier_hd64.md")
+    path = os.path.join(ROOT, "profiles", "k_outlier_px_hd64.md")
     try:
         for line in open(path):
             if line.strip().startswith(key + ":"):
@@ -408,7 +408,8 @@ def run_gpu(args):
     if instr:
         ach = instr / (per_var[0] / 1e3) / 1e9
         issue = {"achieved": ach, "peak": issue_peak, "unit": "G warp instructions/s",
-                 "frac": ach / issue_peak, "kernel": "k_composite<3, 1, 2, 1> (abs average)",
+                 "frac": ach / issue_peak,
+                 "kernel": "k_outlier_px<1, 2, 1, 2, 0, 2> (abs average)",
                  "instructions_per_launch": instr}
     # the reference's CPU algorithm on the same whole stack: two steps on all host threads
     cpu_threads = os.cpu_count() or 1
@@ -434,7 +435,8 @@ def run_gpu(args):
                                      "OutlierProcessor / SimpleProcessor run each)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
-                     "kernel": "k_composite<3> (outlier)", "peak_kind": peak_kind},
+                     "kernel": "k_outlier_px (outlier, mean of the four settings)",
+                     "peak_kind": peak_kind},
         "issue_roofline": issue,
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cpu_threads,
                          "kind": "port", "sample": cpu_desc},
@@ -503,8 +505,9 @@ def _time_device(ctx, lib, fn, steps, warmup):
 
 
 def video_workload(args, ctx, lib, _abi, local, clk=None):
-    """Chrono-video: 300 resident frames of 1920x1080 (brightness drift, one disk on a sine
-    path, generated on the device), 269 windows [f, f+32) with explicit index lists,
+    """Chrono-video: 300 resident frames of 1920x1080 (--video-frames, --video-size; a smaller
+    pool for profiling; brightness drift, one disk on a sine path, generated on the device),
+    269 windows [f, f+32) with explicit index lists,
     abs/0.05/0.2 extreme, background first. Times one cp_composite_video_device call (the
     windows slide by one frame: the sliding-window kernel), the same call with every window
     on the general batched kernel (CP_VIDEO_SLIDING=0), and the plain kernel (one
@@ -512,10 +515,11 @@ def video_workload(args, ctx, lib, _abi, local, clk=None):
     reads every composite and mask back. Returns a dict."""
     import numpy as np
     from chrono_photo_gb300 import example_data, make_params
-    n_pool, win = 300, 32
+    n_pool, win = args.video_frames, 32
+    VW, VH = (int(v) for v in args.video_size.lower().split("x"))
     nwin = n_pool - win + 1
-    fb = W * H * C
-    pool = example_data.video_stack_device(seed=3, n=n_pool, w=W, h=H)
+    fb = VW * VH * C
+    pool = example_data.video_stack_device(seed=3, n=n_pool, w=VW, h=VH)
     dev = pool.data_ptr()
     hptr, _ = _pinned(ctx, lib, n_pool * fb)
     ctx.check(lib.cp_memcpy_d2h(ctx.handle, hptr, dev, n_pool * fb, None))
@@ -532,7 +536,7 @@ def video_workload(args, ctx, lib, _abi, local, clk=None):
 
     def call():
         ctx.check(lib.cp_composite_video_device(
-            ctx.handle, frame_ptrs, n_pool, W, H, C, nwin, starts.ctypes.data_as(_abi.I64P),
+            ctx.handle, frame_ptrs, n_pool, VW, VH, C, nwin, starts.ctypes.data_as(_abi.I64P),
             lens.ctypes.data_as(_abi.I32P), idx.ctypes.data_as(_abi.I32P), ct.byref(p), outs,
             blends, None, None), "cp_composite_video_device")
 
@@ -548,7 +552,7 @@ def video_workload(args, ctx, lib, _abi, local, clk=None):
     for k in range(nwin):
         ptrs = (ct.c_void_p * win)(*[frame_ptrs[k + i] for i in range(win)])
         keep.append(ptrs)
-        wstacks.append(_abi.Stack(n=win, width=W, height=H, channels=C,
+        wstacks.append(_abi.Stack(n=win, width=VW, height=VH, channels=C,
                                   frames=ct.cast(ptrs, ct.POINTER(ct.c_void_p)), frame_offset=k))
 
     def plain():
@@ -570,15 +574,15 @@ def video_workload(args, ctx, lib, _abi, local, clk=None):
     for _ in range(e2e_steps):
         e2e()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    mpxf = nwin * win * W * H / 1e6
+    mpxf = nwin * win * VW * VH / 1e6
     unique = n_pool * fb + 2 * nwin * fb
     peaks, kind = measured_peaks()
     ach = unique / (ms / 1e3) / 1e9
     ctx.free(outs_dev)
     del pool
     return {
-        "workload": "chrono-video: 300 resident 1920x1080 RGB frames, 269 windows of 32 at "
-                    "stride 1, abs/0.05/0.2 extreme, background first",
+        "workload": "chrono-video: %d resident %dx%d RGB frames, %d windows of 32 at "
+                    "stride 1, abs/0.05/0.2 extreme, background first" % (n_pool, VW, VH, nwin),
         "metric": METRIC, "value": mpxf / (ms / 1e3), "unit": METRIC, "ms_per_call": ms,
         "steps": steps, "kernel": "k_video_slide (windows sliding by one frame)",
         "batched_general": {"value": mpxf / (batched_ms / 1e3), "unit": METRIC,
@@ -992,6 +996,9 @@ def main():
                     choices=["hd", "video", "serve", "shake", "ingest"],
                     help="hd (default): the headline line; the others print their own lines")
     ap.add_argument("--jobs", type=int, default=512, help="serve: number of jobs")
+    ap.add_argument("--video-frames", type=int, default=300,
+                    help="video: frames in the resident pool (windows of 32 slide over it)")
+    ap.add_argument("--video-size", default="1920x1080", help="video: frame size WxH")
     ap.add_argument("--no-batched", action="store_true",
                     help="hd: leave out the video and serve sub-objects of the headline line")
     args = ap.parse_args()
