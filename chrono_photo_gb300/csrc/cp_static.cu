@@ -17,7 +17,6 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/chrono_gpu.h"
 #include "cp_host_internal.h"
@@ -56,21 +55,15 @@ __global__ void k_static_fill(const __grid_constant__ FillChunk c, unsigned char
   for (uint32_t i = threadIdx.x; i < c.words; i += blockDim.x) dst[i] = c.data[i];
 }
 
-std::mutex g_setup_mu;
-void* g_scratch_ptr[kMaxStaticDevices] = {};
-
-// Device address of the scratch array on `device` (the current device), looked up once per
-// device with that device current. The host-side name of the array is not a device address.
+// Device address of the scratch array on `device` (the current device), looked up on every
+// call: a cached address would dangle after a device reset or a new primary context, and the
+// lookup is cheap. The host-side name of the array is not a device address.
 int scratch_address(int device, unsigned char** out) {
   if (device < 0 || device >= kMaxStaticDevices) return CP_ERR_ARG;
-  std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (!g_scratch_ptr[device]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess || !p) return CP_ERR_CUDA;
-    g_scratch_ptr[device] = p;
-  }
-  *out = static_cast<unsigned char*>(g_scratch_ptr[device]);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e != cudaSuccess || !p) return CP_ERR_CUDA;
+  *out = static_cast<unsigned char*>(p);
   return CP_OK;
 }
 

@@ -10,7 +10,8 @@
 //   - the tile's frame rows stream through a small ring of shared-memory rows (16-byte
 //     cp.async copies issued kVideoPF frames ahead), each frame read from HBM once per tile
 //     instead of once per window; each lane keeps its pixel's L samples in a shared-memory
-//     ring of words (one word per frame);
+//     ring of words, every frame stored twice (slots s and s + L), so that the window is L
+//     consecutive slots and sample i one load at a fixed offset from the window's first;
 //   - each lane keeps the bit planes of its pixel's window in registers (8 planes per
 //     channel, window position i at bit 32*NW - L + i); sliding the window shifts every
 //     plane down by one and inserts the entering frame's bits at the top (two funnel shifts
@@ -72,8 +73,8 @@ __global__ void __launch_bounds__(32, 16) k_video_slide(const __grid_constant__ 
   const StackDev& S = A.S;
   const int n = S.n;
   const int lane = static_cast<int>(threadIdx.x);
-  uint32_t* ring = reinterpret_cast<uint32_t*>(smem);             // [n][32] pixel words
-  uint8_t* rows = smem + n * 32 * 4;                              // [kVideoPF][row pitch]
+  uint32_t* ring = reinterpret_cast<uint32_t*>(smem);             // [2n][32] pixel words
+  uint8_t* rows = smem + 2 * n * 32 * 4;                          // [kVideoPF][row pitch]
   uint8_t* stage = rows + kVideoPF * kVideoRowPitch;              // [2][row pitch] outputs
   uint32_t wbytes = 0;
 #pragma unroll
@@ -121,6 +122,7 @@ __global__ void __launch_bounds__(32, 16) k_video_slide(const __grid_constant__ 
     for (int j = 0; j < n; ++j) {  // the first window
       const uint32_t x = consume(j);
       ring[j * 32 + lane] = x;
+      ring[(j + n) * 32 + lane] = x;
       planes_push<NW>(P, x);
 #pragma unroll
       for (int ch = 0; ch < C; ++ch) sum[ch] += (x >> (8 * ch)) & 0xFFu;
@@ -132,6 +134,7 @@ __global__ void __launch_bounds__(32, 16) k_video_slide(const __grid_constant__ 
         const int slot = head == 0 ? n - 1 : head - 1;  // the leaving sample's slot
         const uint32_t xo = ring[slot * 32 + lane];
         ring[slot * 32 + lane] = xi;
+        ring[(slot + n) * 32 + lane] = xi;
         planes_push<NW>(P, xi);
 #pragma unroll
         for (int ch = 0; ch < C; ++ch)
@@ -154,11 +157,9 @@ __global__ void __launch_bounds__(32, 16) k_video_slide(const __grid_constant__ 
       }
       const float wq0[C] = {0.0f, 0.0f, 0.0f};
       const PxStat<C> st = px_stat<C>(S, lo3, hi3, wq0);
-      auto load = [&](int i) -> uint32_t {
-        int s = head + i;
-        s = s >= n ? s - n : s;
-        return ring[s * 32 + lane];
-      };
+      // window position i is slot head + i (< 2n): no wrap
+      const uint32_t* win = ring + head * 32 + lane;
+      auto load = [&](int i) -> uint32_t { return win[i * 32]; };
       uint32_t pb[NW];
       int32_t key;
       float dmax;
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(32, 16) k_video_slide(const __grid_constant__ 
 
 }  // namespace
 
-int video_smem_bytes(int n) { return n * 32 * 4 + (kVideoPF + 2) * kVideoRowPitch; }
+int video_smem_bytes(int n) { return 2 * n * 32 * 4 + (kVideoPF + 2) * kVideoRowPitch; }
 
 template <int OG, int BG, int NW>
 static int video_launch_t(const VideoArgs& a, int grid, int smem, void* stream) {
