@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-f
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
 CU_SOURCES = ["cp_kernels_c3.cu", "cp_kernels_c4.cu", "cp_kernels_c1.cu", "cp_shake.cu",
-              "cp_static.cu", "cp_video.cu"]
+              "cp_static.cu", "cp_video.cu", "cp_kernels_multi.cu"]
 # cp_kernels_variant.cu compiled once per specialised single-stack outlier kernel:
 # (channels, distance kind, outlier group, background), the CP_VARIANTS list of cp_internal.h
 KERNEL_VARIANTS = [(3, k, g, b) for k in (1, 2) for b in (1, 0) for g in (1, 2, 3)] + \
@@ -39,7 +39,7 @@ CPP_SOURCES = ["cp_host.cpp", "cp_stage.cpp", "cp_batch.cpp", "cp_shake_host.cpp
                "cp_server.cpp", "cp_ingest.cpp", "cp_png_write.cpp", "cp_tune.cpp",
                "cp_jpeg.cpp", "cp_jpeg_write.cpp"]
 HEADERS = ["cp_internal.h", "cp_host_internal.h", "cp_tile.cuh", "cp_png.h", "cp_pixel.cuh",
-           "cp_outlier_px.cuh", "cp_io.h"]
+           "cp_outlier_px.cuh", "cp_outlier_multi.cuh", "cp_io.h"]
 
 
 def _cuda_home():

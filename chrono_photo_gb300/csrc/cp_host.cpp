@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -356,6 +357,154 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
     }
   }
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "composite launch");
+}
+
+namespace {
+
+// The pixel-thread kernels take the stack (RGB, aligned rows, no crop, integer or paired f32
+// distances); the multi-setting kernel takes those same stacks.
+bool px_eligible(cp_ctx* ctx, const StackDev& d) {
+  return d.mode == CP_MODE_OUTLIER && d.channels == 3 && !d.shifted && !d.has_crop &&
+         (d.fast_int || d.pair_f32) && px_smem_bytes(d.n, false) <= ctx->max_smem &&
+         (d.nw == 1 || d.nw == 2 || d.nw == 4);
+}
+
+// Darker / lighter settings the multi-setting kernel folds on its staged rows: RGB, rows
+// starting 16-byte aligned, no crop.
+bool simple_eligible(const StackDev& d) {
+  return d.mode != CP_MODE_OUTLIER && d.channels == 3 && !d.shifted && !d.has_crop;
+}
+
+// Settings over the same frames and band.
+bool same_stack(const StackDev& a, const StackDev& b) {
+  return a.n == b.n && a.px_begin == b.px_begin && a.px_end == b.px_end && a.tiles == b.tiles &&
+         std::memcmp(a.frames, b.frames, sizeof(a.frames[0]) * static_cast<size_t>(a.n)) == 0;
+}
+
+// Settings whose order statistics are the same: one stack, band and (sub)sample.
+bool same_stats(const StackDev& a, const StackDev& b) {
+  return same_stack(a, b) && a.n_sub == b.n_sub && a.med_k == b.med_k && a.med_pair == b.med_pair &&
+         a.q1_k == b.q1_k && a.q1_pair == b.q1_pair && a.q1_frac == b.q1_frac &&
+         a.q3_k == b.q3_k && a.q3_pair == b.q3_pair && a.q3_frac == b.q3_frac &&
+         std::memcmp(a.sample_mask, b.sample_mask, sizeof a.sample_mask) == 0;
+}
+
+// The fields the distance pass reads (besides the order statistics): equal fields give equal
+// outlier flags and extreme.
+struct DistKey {
+  int32_t thr_abs;
+  uint32_t wmask, fast_int, pair_f32, finite_w, neg_w;
+  float w[4];
+  float thr_sq;
+  int32_t thr_int[5];
+};
+DistKey dist_key(const StackDev& d) {
+  DistKey k;
+  std::memset(&k, 0, sizeof k);
+  k.thr_abs = d.thr_abs;
+  k.wmask = d.wmask;
+  k.fast_int = d.fast_int;
+  k.pair_f32 = d.pair_f32;
+  k.finite_w = d.finite_w;
+  k.neg_w = d.neg_w;
+  std::memcpy(k.w, d.w, sizeof k.w);
+  k.thr_sq = d.thr_sq;
+  std::memcpy(k.thr_int, d.thr_int, sizeof k.thr_int);
+  return k;
+}
+bool operator<(const DistKey& a, const DistKey& b) { return std::memcmp(&a, &b, sizeof a) < 0; }
+bool operator==(const DistKey& a, const DistKey& b) { return std::memcmp(&a, &b, sizeof a) == 0; }
+
+}  // namespace
+
+int launch_multi(cp_ctx* ctx, const std::vector<StackDev>& ds, cudaStream_t stream) {
+  // settings the multi-setting kernel takes together: pixel-kernel stacks with the order
+  // statistics of the first of them; at least two, or there is nothing to share
+  std::vector<size_t> fused, rest, simple;
+  for (size_t i = 0; i < ds.size(); ++i) {
+    const bool ok = px_eligible(ctx, ds[i]) && (fused.empty() || same_stats(ds[fused[0]], ds[i]));
+    (ok ? fused : rest).push_back(i);
+  }
+  if (fused.empty()) {
+    for (size_t i : rest) {
+      const int rc = launch_single(ctx, ds[i], stream);
+      if (rc) return rc;
+    }
+    return CP_OK;
+  }
+  // darker / lighter of the same stack fold the staged rows of the outlier settings' launch
+  // (reading the stack again in their own launch costs more than the fold)
+  for (auto it = rest.begin(); it != rest.end();) {
+    if (simple_eligible(ds[*it]) && same_stack(ds[fused[0]], ds[*it])) {
+      simple.push_back(*it);
+      it = rest.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  // equal distance passes next to each other, so that each runs once; the outlier settings
+  // first (sets[0] gives the launch its sampling), then darker / lighter
+  std::stable_sort(fused.begin(), fused.end(), [&](size_t a, size_t b) {
+    return dist_key(ds[a]) < dist_key(ds[b]);
+  });
+  fused.insert(fused.end(), simple.begin(), simple.end());
+  if (fused.size() < 2) {
+    rest.insert(rest.end(), fused.begin(), fused.end());
+    fused.clear();
+  }
+  std::unique_ptr<MultiArgs> m(new MultiArgs());
+  for (size_t c0 = 0; c0 < fused.size(); c0 += kMultiMax) {
+    const size_t cnt = std::min<size_t>(kMultiMax, fused.size() - c0);
+    if (cnt == 1) {
+      rest.push_back(fused[c0]);
+      continue;
+    }
+    if (ds[fused[c0]].mode != CP_MODE_OUTLIER) {  // a chunk of darker / lighter only
+      for (size_t k = 0; k < cnt; ++k) rest.push_back(fused[c0 + k]);
+      continue;
+    }
+    std::memset(m.get(), 0, sizeof(MultiArgs));
+    bool rel = false;
+    for (size_t k = 0; k < cnt; ++k) {
+      const StackDev& d = ds[fused[c0 + k]];
+      const bool outlier = d.mode == CP_MODE_OUTLIER;
+      m->sets[k] = d;
+      m->share_dist[k] = outlier && k > 0 && ds[fused[c0 + k - 1]].mode == CP_MODE_OUTLIER &&
+                                 dist_key(d) == dist_key(ds[fused[c0 + k - 1]])
+                             ? 1
+                             : 0;
+      rel = rel || (outlier && !d.thr_abs);
+    }
+    m->count = static_cast<int32_t>(cnt);
+    const StackDev& d0 = m->sets[0];
+    const int smem = px_smem_bytes(d0.n, false);
+    int per_sm = 1;
+    {
+      const auto key = std::make_pair(6000 + d0.nw * 2 + (rel ? 1 : 0), smem);
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      auto it = ctx->occupancy.find(key);
+      if (it != ctx->occupancy.end()) {
+        per_sm = it->second;
+      } else {
+        per_sm = std::max(1, px_multi(*m, rel, true, 0, smem, nullptr, nullptr));
+        ctx->occupancy[key] = per_sm;
+      }
+    }
+    const int grid = std::max(1, std::min(d0.tiles, per_sm * ctx->sm_count));
+    const int rc = px_multi(*m, rel, false, grid, smem, stream, ctx->d_error);
+    if (rc < 0) {
+      ctx_error(ctx, "no multi-setting kernel for %d plane words", d0.nw);
+      return CP_ERR_ARG;
+    }
+    const int st = cuda_status(ctx, static_cast<cudaError_t>(rc), "multi-setting launch");
+    if (st) return st;
+  }
+  std::sort(rest.begin(), rest.end());
+  for (size_t i : rest) {
+    const int rc = launch_single(ctx, ds[i], stream);
+    if (rc) return rc;
+  }
+  return CP_OK;
 }
 
 int check_device_error(cp_ctx* ctx) {
@@ -755,6 +904,38 @@ int cp_composite_device(cp_ctx* ctx, const cp_stack* stack, const cp_params* par
   }
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
   return launch_single(ctx, *d, st);
+}
+
+int cp_composite_device_multi(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                              int32_t count, uint8_t* const* out, uint8_t* const* out_blend,
+                              uint64_t* warnings, void* stream) {
+  if (!ctx || !stack || !params || !out || count < 1) return CP_ERR_ARG;
+  if (count > CP_MAX_SETTINGS) return CP_ERR_LIMIT;
+  if (stack->n < 1 || stack->n > CP_MAX_FRAMES || (!stack->frames && !stack->base))
+    return CP_ERR_ARG;
+  for (int32_t k = 0; k < count; ++k)
+    if (!out[k]) return CP_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  try {
+    std::vector<const uint8_t*> fr(static_cast<size_t>(stack->n));
+    for (int i = 0; i < stack->n; ++i)
+      fr[static_cast<size_t>(i)] =
+          stack->frames ? stack->frames[i] : stack->base + stack->frame_stride * i;
+    std::vector<StackDev> ds(static_cast<size_t>(count));
+    for (int32_t k = 0; k < count; ++k) {
+      StackDev& d = ds[static_cast<size_t>(k)];
+      const int rc = prepare_stack(ctx, stack, &params[k], fr.data(), &d);
+      if (rc) return rc;
+      d.out = out[k];
+      d.blend = params[k].mode == CP_MODE_OUTLIER && out_blend ? out_blend[k] : nullptr;
+      d.warnings = warnings ? reinterpret_cast<unsigned long long*>(warnings) + k : nullptr;
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return launch_multi(ctx, ds, st);
+  } catch (const std::exception& e) {
+    ctx_error(ctx, "cp_composite_device_multi: %s", e.what());
+    return CP_ERR_OOM;
+  }
 }
 
 }  // extern "C"

@@ -90,6 +90,9 @@ int fade_lut(const cp_fade* f, int32_t n, int32_t frame_offset, float* out);
 int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
                   const uint8_t* const* dev_frames, StackDev* d);
 int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream);
+// Several settings of one stack (and band): the pixel-kernel settings sharing their order
+// statistics in multi-setting launches of up to kMultiMax, the rest one by one.
+int launch_multi(cp_ctx* ctx, const std::vector<StackDev>& ds, cudaStream_t stream);
 // The pixel-thread kernel with its measured (or cached, forced, static) configuration.
 int launch_px(cp_ctx* ctx, const StackDev& d, cudaStream_t stream);
 int check_device_error(cp_ctx* ctx);

@@ -182,6 +182,23 @@ struct PxAux {
 inline int px_smem_bytes(int n, bool db) {
   return kSmemHeader + (db ? 2 : 1) * n * row_pitch_host(3) + static_cast<int>(sizeof(PxAux));
 }
+// Several outlier settings of one stack in one pass (k_outlier_multi, cp_outlier_multi.cuh):
+// the settings' descriptors, kernel parameters; sets[0] also gives the frames, geometry and
+// (sub)sample, which all of them share. share_dist[s]: setting s has the distance kind,
+// threshold and weights of setting s - 1, so its outlier flags and extreme are the same.
+constexpr int kMultiMax = 8;
+struct MultiArgs {
+  StackDev sets[kMultiMax];
+  int32_t count;
+  int32_t share_dist[kMultiMax];
+  int32_t pad[3];
+};
+static_assert(sizeof(MultiArgs) <= 32764, "MultiArgs exceeds the kernel parameter limit");
+// Launch (occupancy_only: CTAs per SM instead) of the multi-setting kernel for the plane
+// words of a.sets[0]; rel: some setting has a rel threshold (quartiles needed).
+int px_multi(const MultiArgs& a, bool rel, bool occupancy_only, int grid, int smem, void* stream,
+             uint32_t* error);
+
 // (distance kind, outlier group, background) of the compiled pixel-thread kernels; each
 // translation unit holds plane-word counts 1 and 2 (single and double buffered) and 4
 // (single), each with phase A by word column (pa 0) and by pixel (pa 2).

@@ -52,15 +52,10 @@ DEVI PxStat<C> px_stat(const StackDev& S, uint32_t lo3, uint32_t hi3, const floa
   return r;
 }
 
-// Order statistics of one pixel from its own samples: bit planes of the C channel bytes of
-// each sample word (8x8 bit transposes of 8 samples, then a byte transpose of 4 groups),
-// radix selections of the median pair and, for rel thresholds, the quartiles
-// (src/chrono.rs:220-255). lo3 / hi3 as for px_stat; wq = w * iqr_inv; q1v / q3v the
-// quartiles (debug outputs).
-template <int C, int NW, int KIND, typename Load>
-DEVI void pixel_order_stats(const StackDev& S, int n, Load load, uint32_t& lo3, uint32_t& hi3,
-                            float (&wq)[C], float (&q1v)[C], float (&q3v)[C]) {
-  uint32_t P[C][8][NW];
+// Bit planes of one pixel's samples: P[ch][r][blk] bit i = bit r of channel byte ch of sample
+// 32*blk + i (8x8 bit transposes of 8 samples, then a 4x4 byte transpose of 4 groups).
+template <int C, int NW, typename Load>
+DEVI void pixel_planes(int n, Load load, uint32_t (&P)[C][8][NW]) {
 #pragma unroll
   for (int blk = 0; blk < NW; ++blk) {
     uint32_t a[4][8];
@@ -83,9 +78,12 @@ DEVI void pixel_order_stats(const StackDev& S, int n, Load load, uint32_t& lo3, 
       if (C > 3) P[3 % C][r][blk] = __byte_perm(t1, t3, 0x7632);
     }
   }
-  uint32_t smask[NW];
-#pragma unroll
-  for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
+}
+
+// d[k] and d[k+1] (or d[k] again without a pair) of the median per channel byte.
+template <int C, int NW>
+DEVI void pixel_median_pair(const StackDev& S, const uint32_t (&P)[C][8][NW],
+                            const uint32_t (&smask)[NW], uint32_t& lo3, uint32_t& hi3) {
   uint32_t lo[C], hi[C];
   select_rank<NW, C>(P, smask, S.med_k, lo);
   if (S.med_pair) {
@@ -100,26 +98,58 @@ DEVI void pixel_order_stats(const StackDev& S, int n, Load load, uint32_t& lo3, 
   for (int ch = 0; ch < C; ++ch) {
     lo3 |= lo[ch] << (8 * ch);
     hi3 |= hi[ch] << (8 * ch);
+  }
+}
+
+// Quartiles and 1 / iqr per channel, src/chrono.rs:246-252 (iqr 0 counts as 1).
+template <int C, int NW>
+DEVI void pixel_quartiles(const StackDev& S, const uint32_t (&P)[C][8][NW],
+                          const uint32_t (&smask)[NW], float (&q1v)[C], float (&q3v)[C],
+                          float (&iqr_inv)[C]) {
+  uint32_t a1[C], b1[C], a3[C], b3[C];
+  select_rank<NW, C>(P, smask, S.q1_k, a1);
+  if (S.q1_pair) select_rank<NW, C>(P, smask, S.q1_k + 1, b1);
+  select_rank<NW, C>(P, smask, S.q3_k, a3);
+  if (S.q3_pair) select_rank<NW, C>(P, smask, S.q3_k + 1, b3);
+#pragma unroll
+  for (int ch = 0; ch < C; ++ch) {
+    const float q1 = quantile_value(a1[ch], S.q1_pair ? b1[ch] : a1[ch], S.q1_pair != 0, S.q1_frac);
+    const float q3 = quantile_value(a3[ch], S.q3_pair ? b3[ch] : a3[ch], S.q3_pair != 0, S.q3_frac);
+    float iqr = __fsub_rn(q3, q1);
+    if (iqr == 0.0f) iqr = 1.0f;
+    iqr_inv[ch] = __fdiv_rn(1.0f, iqr);
+    q1v[ch] = q1;
+    q3v[ch] = q3;
+  }
+}
+
+// Order statistics of one pixel from its own samples: bit planes, radix selections of the
+// median pair and, for rel thresholds, the quartiles (src/chrono.rs:220-255). lo3 / hi3 as
+// for px_stat; wq = w * iqr_inv; q1v / q3v the quartiles (debug outputs).
+template <int C, int NW, int KIND, typename Load>
+DEVI void pixel_order_stats(const StackDev& S, int n, Load load, uint32_t& lo3, uint32_t& hi3,
+                            float (&wq)[C], float (&q1v)[C], float (&q3v)[C]) {
+  uint32_t P[C][8][NW];
+  pixel_planes<C, NW>(n, load, P);
+  uint32_t smask[NW];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
+  pixel_median_pair<C, NW>(S, P, smask, lo3, hi3);
+#pragma unroll
+  for (int ch = 0; ch < C; ++ch) {
     wq[ch] = 0.0f;
     q1v[ch] = 0.0f;
     q3v[ch] = 0.0f;
   }
   if (KIND != kIntKind && !S.thr_abs) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
-    uint32_t a1[C], b1[C], a3[C], b3[C];
-    select_rank<NW, C>(P, smask, S.q1_k, a1);
-    if (S.q1_pair) select_rank<NW, C>(P, smask, S.q1_k + 1, b1);
-    select_rank<NW, C>(P, smask, S.q3_k, a3);
-    if (S.q3_pair) select_rank<NW, C>(P, smask, S.q3_k + 1, b3);
+    float iqr_inv[C], q1[C], q3[C];
+    pixel_quartiles<C, NW>(S, P, smask, q1, q3, iqr_inv);
 #pragma unroll
     for (int ch = 0; ch < C; ++ch) {
-      const float q1 = quantile_value(a1[ch], S.q1_pair ? b1[ch] : a1[ch], S.q1_pair != 0, S.q1_frac);
-      const float q3 = quantile_value(a3[ch], S.q3_pair ? b3[ch] : a3[ch], S.q3_pair != 0, S.q3_frac);
-      float iqr = __fsub_rn(q3, q1);
-      if (iqr == 0.0f) iqr = 1.0f;
-      wq[ch] = __fmul_rn(S.w[ch], __fdiv_rn(1.0f, iqr));
+      wq[ch] = __fmul_rn(S.w[ch], iqr_inv[ch]);
       const bool wt = (S.wmask >> ch) & 1u;
-      q1v[ch] = wt ? q1 : 0.0f;
-      q3v[ch] = wt ? q3 : 0.0f;
+      q1v[ch] = wt ? q1[ch] : 0.0f;
+      q3v[ch] = wt ? q3[ch] : 0.0f;
     }
   }
 }
@@ -229,6 +259,45 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
       pb[blk] = ob;
     }
   }
+}
+
+// SimpleProcessor's fold for one pixel (src/simple.rs:96-133), over samples 0..n-1: running
+// extreme of sum_c p_c * w_c (f32, c ascending, strict compare: the earliest sample wins
+// ties); on a new extreme the sample is blended into the running output (starting at 0) with
+// its fade. With 0/1 weights and every fade factor >= 1 the sums are exact integers (dp4a)
+// and a new extreme copies the sample.
+template <int C, typename Load>
+DEVI uint32_t px_simple(const StackDev& S, int n, Load load) {
+  const bool darker = S.mode == CP_MODE_DARKER;
+  uint32_t outw = 0u;
+  if (S.unit_w && S.no_fade) {
+    uint32_t ones = 0u;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch)
+      if ((S.wmask >> ch) & 1u) ones |= 1u << (8 * ch);
+    int32_t ext = darker ? 0x7FFFFFFF : -1;
+    for (int i = 0; i < n; ++i) {
+      const uint32_t px = load(i) & (0xFFFFFFFFu >> (32 - 8 * C));
+      const int32_t v = static_cast<int32_t>(__dp4a(px, ones, 0u));
+      const bool up = darker ? (v < ext) : (v > ext);
+      ext = up ? v : ext;
+      outw = up ? px : outw;
+    }
+    return outw;
+  }
+  float ext = darker ? FLT_MAX : -FLT_MAX;
+  for (int i = 0; i < n; ++i) {
+    const uint32_t px = load(i) & (0xFFFFFFFFu >> (32 - 8 * C));
+    float value = 0.0f;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch)
+      value = __fadd_rn(value, __fmul_rn(u8f((px >> (8 * ch)) & 0xFFu), S.w[ch]));
+    const bool up = darker ? (value < ext) : (value > ext);
+    ext = up ? value : ext;
+    const float fade = S.fade[i];
+    if (up && fade > 0.0f) outw = fade >= 1.0f ? px : blend_into_u8<C>(outw, px, fade);
+  }
+  return outw;
 }
 
 struct PxOut {

@@ -140,8 +140,8 @@ static int composite_staged(cp_ctx* ctx, const cp_stack* stack, const cp_params*
   // bands: flat pixel ranges in whole tiles; cropped stacks move whole frames at once
   int bands = 1;
   if (!crop && P >= static_cast<uint64_t>(kTilePx) * ctx->sm_count * 4) bands = 4;
-  // per band: two copies landed, then one kernel done per setting
-  const int ev_band = 2 + count;
+  // per band: two copies landed, then the band's kernels done
+  const int ev_band = 3;
   rc = ensure_events(ctx, static_cast<size_t>(ev_band * bands));
   if (rc) return rc;
   const uint64_t tiles_total = (P + kTilePx - 1) / kTilePx;
@@ -190,18 +190,23 @@ static int composite_staged(cp_ctx* ctx, const cp_stack* stack, const cp_params*
     cudaStreamWaitEvent(ctx->stream, copied, 0);
     cudaStreamWaitEvent(ctx->stream, copied2, 0);
     const uint64_t o0 = crop ? 0 : px0 * C, ob = crop ? out_bytes : (px1 - px0) * C;
-    for (int k = 0; k < count; ++k) {
-      StackDev db = ds[static_cast<size_t>(k)];
+    // the band under every setting: settings sharing their order statistics in one
+    // multi-setting launch (cp_outlier_multi.cuh), then every result back
+    std::vector<StackDev> band(ds);
+    for (StackDev& db : band) {
       if (!crop) {
         db.px_begin = static_cast<int32_t>(px0);
         db.px_end = static_cast<int32_t>(px1);
         db.tiles = static_cast<int32_t>(t1 - t0);
       }
-      rc = launch_single(ctx, db, ctx->stream);
-      if (rc) return rc;
-      cudaEvent_t done = ctx->band_events[static_cast<size_t>(ev_band * b + 2 + k)];
-      cudaEventRecord(done, ctx->stream);
-      cudaStreamWaitEvent(ctx->d2h_stream, done, 0);
+    }
+    rc = launch_multi(ctx, band, ctx->stream);
+    if (rc) return rc;
+    cudaEvent_t done = ctx->band_events[static_cast<size_t>(ev_band * b + 2)];
+    cudaEventRecord(done, ctx->stream);
+    cudaStreamWaitEvent(ctx->d2h_stream, done, 0);
+    for (int k = 0; k < count; ++k) {
+      const StackDev& db = band[static_cast<size_t>(k)];
       rc = cuda_status(ctx, cudaMemcpyAsync(outs[k] + o0, db.out + o0, ob,
                                             cudaMemcpyDeviceToHost, ctx->d2h_stream), "d2h");
       if (!rc && db.blend)

@@ -214,6 +214,19 @@ int cp_composite_device(cp_ctx* ctx, const cp_stack* stack, const cp_params* par
                         uint8_t* out, uint8_t* out_blend, const cp_debug* dbg,
                         uint64_t* warnings, void* stream);
 
+/* One device-resident stack under `count` parameter sets (at most CP_MAX_SETTINGS), the
+ * device form of cp_composite_multi: out[k], out_blend[k] (nullable; outlier settings only)
+ * and warnings[k] (device uint64 array of count entries, nullable) as for
+ * cp_composite_device with params[k]. Outlier settings that share the stack's order
+ * statistics (RGB frames starting 16-byte aligned, integer or paired-f32 distances, the
+ * same --sample) run in one multi-setting pass that stages every frame row and selects the
+ * medians once for all of them; each setting's results equal cp_composite_device's for it
+ * alone. Replaces several OutlierProcessor::process runs over the same files
+ * (src/main.rs:465-483 once per setting). */
+int cp_composite_device_multi(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
+                              int32_t count, uint8_t* const* out, uint8_t* const* out_blend,
+                              uint64_t* warnings, void* stream);
+
 /* Host-memory form of cp_composite_device: frames in host memory are staged through
  * pinned buffers and copied to the device in row bands that overlap the kernel; results
  * are copied back. Synchronous. n_warnings (host, nullable) receives the warning count.
