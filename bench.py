@@ -392,6 +392,8 @@ def run_gpu(args):
         ctx.synchronize()
         barrier()
         torch.cuda.synchronize()
+        launches0 = ct.c_uint64()
+        ctx.check(lib.cp_ctx_launch_counts(h, ct.byref(launches0), None, None))
         start.record(stream)
         for _ in range(args.steps):
             device_step_multi()
@@ -399,6 +401,8 @@ def run_gpu(args):
         ctx.synchronize()
         torch.cuda.synchronize()
         ms_multi = start.elapsed_time(stop)
+        launches1 = ct.c_uint64()
+        ctx.check(lib.cp_ctx_launch_counts(h, ct.byref(launches1), None, None))
     barrier()
     ms_single_max = barrier_max(ms)
     ms_max = barrier_max(ms_multi)
@@ -496,7 +500,8 @@ def run_gpu(args):
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cpu_threads,
                          "kind": "port", "sample": cpu_desc},
         "clocks": clk_summary,
-        "gpu_launches": args.steps,  # one multi-setting launch per step
+        # the library's own count of the kernels it launched in the timed region
+        "gpu_launches": launches1.value - launches0.value,
         "autotune": tuning_report(ctx, lib, _abi),
     }
     if not args.no_batched:

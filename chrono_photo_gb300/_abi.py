@@ -107,6 +107,7 @@ SIGNATURES = [
                                       ct.POINTER(P), ct.POINTER(P), U64P]),
     ("cp_composite_device_multi", ct.c_int, [P, ct.POINTER(Stack), ct.POINTER(Params), I32,
                                              ct.POINTER(P), ct.POINTER(P), P, P]),
+    ("cp_ctx_launch_counts", ct.c_int, [P, U64P, U64P, U64P]),
     ("cp_composite_batch_device", ct.c_int, [P, ct.POINTER(Stack), ct.POINTER(Params), I32,
                                              ct.POINTER(P), ct.POINTER(P), P, P]),
     ("cp_composite_video_device", ct.c_int, [P, ct.POINTER(P), I32, I32, I32, I32, I32, I64P,

@@ -98,6 +98,10 @@ int launch_batch_dispatch(cp_ctx* ctx, const std::vector<StackDev>& host, const 
       default: rc = launch_batch_c4(d_stacks, d_prefix, n, total, interleave, d_counter, err, grid, smem, st); break;
     }
   }
+  // a launch captured into a batch plan's graph counts when the graph is replayed
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cap);
+  if (cap == cudaStreamCaptureStatusNone) count_launches(ctx, 1);
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "batch launch");
 }
 
@@ -248,6 +252,7 @@ static int batch_run(cp_ctx* ctx, const cp_stack* stacks, const cp_params* param
     ctx->plans.push_back(std::move(np));
     plan = ctx->plans.back().get();
   }
+  count_launches(ctx, 1);  // the graph holds one kernel (after the counter reset)
   return cuda_status(ctx, cudaGraphLaunch(plan->exec, st), "graph launch");
 }
 
@@ -366,6 +371,7 @@ static int video_sliding(cp_ctx* ctx, const uint8_t* const* frames, int32_t imag
       }
       A->warnings = warnings ? reinterpret_cast<unsigned long long*>(warnings + k0) : nullptr;
       rc = video_slide(A, og, bg_first, false, grid, smem, st, ctx->d_error);
+      count_launches(ctx, 1);
       if (rc) return cuda_status(ctx, static_cast<cudaError_t>(rc), "sliding-window launch");
     }
     for (int w = k; w < e; ++w) done[static_cast<size_t>(w)] = 1;

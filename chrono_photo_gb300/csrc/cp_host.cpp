@@ -295,6 +295,7 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
       case 3: rc = launch_simple_stream_c3(d, fast, grid, stream, ctx->d_error); break;
       default: rc = launch_simple_stream_c4(d, fast, grid, stream, ctx->d_error); break;
     }
+    count_launches(ctx, 1);
     return cuda_status(ctx, static_cast<cudaError_t>(rc), "simple launch");
   }
   if (d.mode == CP_MODE_OUTLIER && d.channels == 3 && !d.shifted && !d.has_crop &&
@@ -356,6 +357,7 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
       default: rc = launch_composite_c4(d, grid, smem, stream, ctx->d_error); break;
     }
   }
+  count_launches(ctx, 1);
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "composite launch");
 }
 
@@ -381,11 +383,10 @@ bool same_stack(const StackDev& a, const StackDev& b) {
          std::memcmp(a.frames, b.frames, sizeof(a.frames[0]) * static_cast<size_t>(a.n)) == 0;
 }
 
-// Settings whose order statistics are the same: one stack, band and (sub)sample.
+// Settings whose order statistics are the same: one stack, band and (sub)sample (the
+// quartile ranks follow from the sample size; prepare_stack fills them for rel settings).
 bool same_stats(const StackDev& a, const StackDev& b) {
   return same_stack(a, b) && a.n_sub == b.n_sub && a.med_k == b.med_k && a.med_pair == b.med_pair &&
-         a.q1_k == b.q1_k && a.q1_pair == b.q1_pair && a.q1_frac == b.q1_frac &&
-         a.q3_k == b.q3_k && a.q3_pair == b.q3_pair && a.q3_frac == b.q3_frac &&
          std::memcmp(a.sample_mask, b.sample_mask, sizeof a.sample_mask) == 0;
 }
 
@@ -476,6 +477,20 @@ int launch_multi(cp_ctx* ctx, const std::vector<StackDev>& ds, cudaStream_t stre
       rel = rel || (outlier && !d.thr_abs);
     }
     m->count = static_cast<int32_t>(cnt);
+    if (rel) {  // the kernel selects the quartiles with the ranks of sets[0]
+      for (size_t k = 0; k < cnt; ++k) {
+        const StackDev& d = m->sets[k];
+        if (d.mode != CP_MODE_OUTLIER || d.thr_abs) continue;
+        StackDev& d0w = m->sets[0];
+        d0w.q1_k = d.q1_k;
+        d0w.q1_pair = d.q1_pair;
+        d0w.q1_frac = d.q1_frac;
+        d0w.q3_k = d.q3_k;
+        d0w.q3_pair = d.q3_pair;
+        d0w.q3_frac = d.q3_frac;
+        break;
+      }
+    }
     const StackDev& d0 = m->sets[0];
     const int smem = px_smem_bytes(d0.n, false);
     int per_sm = 1;
@@ -498,6 +513,9 @@ int launch_multi(cp_ctx* ctx, const std::vector<StackDev>& ds, cudaStream_t stre
     }
     const int st = cuda_status(ctx, static_cast<cudaError_t>(rc), "multi-setting launch");
     if (st) return st;
+    count_launches(ctx, 1);
+    ctx->n_multi += 1;
+    ctx->n_multi_settings += cnt;
   }
   std::sort(rest.begin(), rest.end());
   for (size_t i : rest) {
@@ -904,6 +922,15 @@ int cp_composite_device(cp_ctx* ctx, const cp_stack* stack, const cp_params* par
   }
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
   return launch_single(ctx, *d, st);
+}
+
+int cp_ctx_launch_counts(cp_ctx* ctx, uint64_t* launches, uint64_t* multi_launches,
+                         uint64_t* multi_settings) {
+  if (!ctx) return CP_ERR_ARG;
+  if (launches) *launches = ctx->n_launches.load();
+  if (multi_launches) *multi_launches = ctx->n_multi.load();
+  if (multi_settings) *multi_settings = ctx->n_multi_settings.load();
+  return CP_OK;
 }
 
 int cp_composite_device_multi(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,

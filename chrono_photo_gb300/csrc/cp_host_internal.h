@@ -68,6 +68,9 @@ struct cp_ctx {
   uint32_t* d_error = nullptr;               // device error flags of bounded waits
   int64_t wait_cycles = 0;                   // bounded-wait limit of launches (0: default)
   std::atomic<int> fail_allocs{0};           // injected failures of the next allocations
+  // kernel launches made by the context (graph replays count one), multi-setting launches
+  // and the settings they carried (cp_ctx_launch_counts)
+  std::atomic<uint64_t> n_launches{0}, n_multi{0}, n_multi_settings{0};
   std::string gpu_name;                      // device name (tuning cache key)
   std::map<int, cp::PxChoice> px_tuned;      // pixel-thread kernel choices by key
   bool tune_loaded = false;                  // the tuning cache file has been read
@@ -90,6 +93,7 @@ int fade_lut(const cp_fade* f, int32_t n, int32_t frame_offset, float* out);
 int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
                   const uint8_t* const* dev_frames, StackDev* d);
 int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream);
+inline void count_launches(cp_ctx* ctx, uint64_t n) { ctx->n_launches += n; }
 // Several settings of one stack (and band): the pixel-kernel settings sharing their order
 // statistics in multi-setting launches of up to kMultiMax, the rest one by one.
 int launch_multi(cp_ctx* ctx, const std::vector<StackDev>& ds, cudaStream_t stream);

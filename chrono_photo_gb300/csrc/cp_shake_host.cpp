@@ -51,9 +51,11 @@ extern "C" int cp_shake_analyze_device(cp_ctx* ctx, const uint8_t* const* frames
   if (e == cudaSuccess && n_anchors > 0)
     e = cudaMemcpyAsync(d_anchors, anchors, 8ull * n_anchors, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_diffs, 0, 4 * nd, st);
-  if (e == cudaSuccess && n_anchors > 0)
+  if (e == cudaSuccess && n_anchors > 0) {
     e = static_cast<cudaError_t>(launch_shake(d_frames, n, width, height, channels, d_anchors,
                                               n_anchors, r, s, d_diffs, st));
+    count_launches(ctx, 1);
+  }
   if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d_diffs, 4 * nd, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   dev_free(ctx, scratch);

@@ -94,6 +94,7 @@ int px_run(cp_ctx* ctx, int k, int g, int b, const StackDev& d, const PxChoice& 
     ctx_error(ctx, "no pixel-thread kernel for variant %d/%d/%d", k, g, b);
     return CP_ERR_ARG;
   }
+  count_launches(ctx, 1);
   return cuda_status(ctx, static_cast<cudaError_t>(rc), "composite launch");
 }
 

@@ -226,6 +226,10 @@ int cp_composite_device(cp_ctx* ctx, const cp_stack* stack, const cp_params* par
 int cp_composite_device_multi(cp_ctx* ctx, const cp_stack* stack, const cp_params* params,
                               int32_t count, uint8_t* const* out, uint8_t* const* out_blend,
                               uint64_t* warnings, void* stream);
+/* Kernel launches the context has made so far (a replayed batch graph counts one), and of
+ * them the multi-setting launches and the settings they carried (any pointer nullable). */
+int cp_ctx_launch_counts(cp_ctx* ctx, uint64_t* launches, uint64_t* multi_launches,
+                         uint64_t* multi_settings);
 
 /* Host-memory form of cp_composite_device: frames in host memory are staged through
  * pinned buffers and copied to the device in row bands that overlap the kernel; results

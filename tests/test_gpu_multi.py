@@ -166,3 +166,27 @@ def test_device_multi_arguments(ctx):
                                          _abi.CP_MAX_SETTINGS + 1, om, None, None,
                                          None) == _abi.CP_ERR_LIMIT
     del frames
+
+
+def launch_counts(ctx):
+    a, b, c = ct.c_uint64(), ct.c_uint64(), ct.c_uint64()
+    ctx.check(_abi.lib().cp_ctx_launch_counts(ctx.handle, ct.byref(a), ct.byref(b), ct.byref(c)))
+    return a.value, b.value, c.value
+
+
+def test_benchmark_step_is_one_launch(ctx):
+    """The benchmark's six settings (abs and rel thresholds, darker, lighter) of one aligned
+    RGB stack take one multi-setting launch carrying all six; a setting with its own sample
+    runs apart."""
+    rng = np.random.default_rng(15)
+    frames = cases.random_stack(rng, 64, 32, 64, 3, n_spots=3)
+    ps = [cases.params(**kw) for kw in bench_six()]
+    l0, m0, s0 = launch_counts(ctx)
+    device_multi(ctx, frames, ps)
+    l1, m1, s1 = launch_counts(ctx)
+    assert (l1 - l0, m1 - m0, s1 - s0) == (1, 1, 6)
+    other = cases.params(mode="outlier", threshold="abs/0.05/0.2", outlier="first",
+                         background="first", sample=list(range(0, 64, 2)))
+    device_multi(ctx, frames, ps + [other])
+    l2, m2, s2 = launch_counts(ctx)
+    assert (l2 - l1, m2 - m1, s2 - s1) == (2, 1, 6)
