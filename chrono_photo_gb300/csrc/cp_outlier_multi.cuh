@@ -120,8 +120,8 @@ __global__ void __launch_bounds__(kPxThreads, kMultiMinCtas<NW>)
           wq[ch] = T.thr_abs ? 0.0f : __fmul_rn(T.w[ch], iqr_inv[ch]);
         const PxStat<C> st = px_stat<C>(T, lo3, hi3, wq);
         if (!M.share_dist[s])
-          px_distance<C, NW, kAnyKind, kOgAny>(T, n, st, wbytes, load, pb, key, dmax, imax);
-        r = px_epilogue<C, NW, kAnyKind, kOgAny, kBgAny>(T, n, st, wbytes, pb, key, dmax, imax,
+          px_distance<C, NW, kPxKind, kOgAny>(T, n, st, wbytes, load, pb, key, dmax, imax);
+        r = px_epilogue<C, NW, kPxKind, kOgAny, kBgAny>(T, n, st, wbytes, pb, key, dmax, imax,
                                                          pix_idx, nullptr, load);
       }
       const int b = s & 1;

@@ -167,7 +167,7 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
   key = st.nh > 0 ? -1 : 255;
   dmax = 0.0f;
   imax = 0;
-  if (KIND == kIntKind || (KIND == kAnyKind && S.fast_int)) {
+  if (KIND == kIntKind || ((KIND == kAnyKind || KIND == kPxKind) && S.fast_int)) {
     const int32_t thr1 = S.thr_int[st.nh] - 1;
 #pragma unroll
     for (int blk = 0; blk < NW; ++blk) {
@@ -186,7 +186,7 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
       }
       pb[blk] = iend > i0 ? __brev(ob) >> (32 - (iend - i0)) : 0u;
     }
-  } else if (KIND == kF32Kind || (KIND == kAnyKind && S.pair_f32)) {
+  } else if (KIND == kF32Kind || KIND == kPxKind || (KIND == kAnyKind && S.pair_f32)) {
     // two samples per instruction in float2 lanes, every term on (median - p) / 2: the
     // sample -(2^14 + p/2) is one byte permute of the pixel byte into -2^14's mantissa, the
     // median 2^14 + median/2 is exact, so terms, sums and the threshold are the reference's
@@ -317,12 +317,14 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
                        int pix_idx, const uint32_t* sums, Load load_raw) {
   PxOut r;
   auto load = [&](int i) -> uint32_t { return load_raw(i) & (0xFFFFFFFFu >> (32 - 8 * C)); };
-  const bool fast = KIND == kIntKind || (KIND == kAnyKind && S.fast_int);
+  const bool fast = KIND == kIntKind || ((KIND == kAnyKind || KIND == kPxKind) && S.fast_int);
   auto dsq_px = [&](uint32_t px) -> float {  // dist_sq of a sample, recomputed
     if (fast)
       return static_cast<float>(dist_int(px, wbytes, st.klo, st.khi)) +
              0.25f * static_cast<float>(st.nh);
-    if constexpr (KIND == kF32Kind) return dist_f32<C, true, false>(S, st.medo, st.wi, px);
+    // paired-f32 stacks have finite, non-negative weights (host-checked)
+    if constexpr (KIND == kF32Kind || KIND == kPxKind)
+      return dist_f32<C, true, false>(S, st.medo, st.wi, px);
     return S.finite_w ? dist_f32<C, true>(S, st.medo, st.wi, px)
                       : dist_f32<C, false>(S, st.medo, st.wi, px);
   };

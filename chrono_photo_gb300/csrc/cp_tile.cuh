@@ -538,10 +538,12 @@ DEVI void store_rows(uint8_t* out, const TileGeo& g, const uint32_t (&rows)[C][3
 // the kind of its distance arithmetic, so each kernel holds only the code it runs (smaller
 // instruction footprint, register allocation of its own).
 // Kinds: kIntKind (abs, 0/1 weights: integer distances), kF32Kind (paired f32 distances),
-// kF32GenKind (scalar f32 distances). Likewise the outlier group (OG) fixes the epilogue:
+// kF32GenKind (scalar f32 distances), kPxKind (integer or paired f32 by the stack's flags,
+// never scalar: the settings of a multi-setting launch). Likewise the outlier group (OG)
+// fixes the epilogue:
 // kOgSingle (extreme / first / last: one sample), kOgAverage, kOgBlend (forward / backward),
 // or kOgAny; and BG the background: kBgFirst or kBgAny.
-enum : int { kAnyKind = 0, kIntKind = 1, kF32Kind = 2, kF32GenKind = 3 };
+enum : int { kAnyKind = 0, kIntKind = 1, kF32Kind = 2, kF32GenKind = 3, kPxKind = 4 };
 enum : int { kOgAny = 0, kOgSingle = 1, kOgAverage = 2, kOgBlend = 3 };
 enum : int { kBgAny = 0, kBgFirst = 1 };
 template <int KIND>
