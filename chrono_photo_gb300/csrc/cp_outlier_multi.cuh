@@ -87,10 +87,11 @@ __global__ void __launch_bounds__(kPxThreads, kMultiMinCtas<NW>)
       uint32_t smask[NW];
 #pragma unroll
       for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
-      pixel_median_pair<C, NW>(S, P, smask, lo3, hi3);
+      uint32_t q1a, q1b, q3a, q3b;
+      pixel_ranks<C, NW, REL>(S, P, smask, REL, lo3, hi3, q1a, q1b, q3a, q3b);
       if (REL) {
         float q1[C], q3[C];
-        pixel_quartiles<C, NW>(S, P, smask, q1, q3, iqr_inv);
+        quartiles_from_ranks<C>(S, q1a, q1b, q3a, q3b, q1, q3, iqr_inv);
       } else {
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) iqr_inv[ch] = 1.0f;

@@ -80,41 +80,52 @@ DEVI void pixel_planes(int n, Load load, uint32_t (&P)[C][8][NW]) {
   }
 }
 
-// d[k] and d[k+1] (or d[k] again without a pair) of the median per channel byte.
-template <int C, int NW>
-DEVI void pixel_median_pair(const StackDev& S, const uint32_t (&P)[C][8][NW],
-                            const uint32_t (&smask)[NW], uint32_t& lo3, uint32_t& hi3) {
-  uint32_t lo[C], hi[C];
-  select_rank<NW, C>(P, smask, S.med_k, lo);
-  if (S.med_pair) {
-    select_rank<NW, C>(P, smask, S.med_k + 1, hi);
-  } else {
+// The median pair and, with QUART, the quartile pairs of one pixel through ONE copy of the
+// selection code: a runtime loop over the needed ranks (med_k, med_k + 1 if paired, q1_k,
+// q1_k + 1, q3_k, q3_k + 1 if paired) instead of one inlined selection per rank (six for rel
+// thresholds, each some 300 instructions: their code footprint stalled instruction fetch).
+// Results are packed per rank (channel byte ch at bits 8ch) and kept in named registers
+// through uniform selects, so no array is indexed at run time.
+// quart: the quartiles are wanted (QUART compiles them in).
+template <int C, int NW, bool QUART>
+DEVI void pixel_ranks(const StackDev& S, const uint32_t (&P)[C][8][NW],
+                      const uint32_t (&smask)[NW], bool quart, uint32_t& lo3, uint32_t& hi3,
+                      uint32_t& q1a, uint32_t& q1b, uint32_t& q3a, uint32_t& q3b) {
+  lo3 = hi3 = q1a = q1b = q3a = q3b = 0u;
+  const int nrank = QUART && quart ? 6 : 2;
+#pragma unroll 1
+  for (int j = 0; j < nrank; ++j) {
+    const bool need = j == 0 || (j == 1 && S.med_pair) || j == 2 || (j == 3 && S.q1_pair) ||
+                      j == 4 || (j == 5 && S.q3_pair);
+    if (!need) continue;
+    const int k = j < 2 ? S.med_k + j : (j < 4 ? S.q1_k + j - 2 : S.q3_k + j - 4);
+    uint32_t v[C];
+    select_rank<NW, C>(P, smask, k, v);
+    uint32_t packed = 0u;
 #pragma unroll
-    for (int ch = 0; ch < C; ++ch) hi[ch] = lo[ch];
+    for (int ch = 0; ch < C; ++ch) packed |= v[ch] << (8 * ch);
+    lo3 = j == 0 ? packed : lo3;
+    hi3 = j == 1 ? packed : hi3;
+    q1a = j == 2 ? packed : q1a;
+    q1b = j == 3 ? packed : q1b;
+    q3a = j == 4 ? packed : q3a;
+    q3b = j == 5 ? packed : q3b;
   }
-  lo3 = 0u;
-  hi3 = 0u;
-#pragma unroll
-  for (int ch = 0; ch < C; ++ch) {
-    lo3 |= lo[ch] << (8 * ch);
-    hi3 |= hi[ch] << (8 * ch);
-  }
+  if (!S.med_pair) hi3 = lo3;
 }
 
-// Quartiles and 1 / iqr per channel, src/chrono.rs:246-252 (iqr 0 counts as 1).
-template <int C, int NW>
-DEVI void pixel_quartiles(const StackDev& S, const uint32_t (&P)[C][8][NW],
-                          const uint32_t (&smask)[NW], float (&q1v)[C], float (&q3v)[C],
-                          float (&iqr_inv)[C]) {
-  uint32_t a1[C], b1[C], a3[C], b3[C];
-  select_rank<NW, C>(P, smask, S.q1_k, a1);
-  if (S.q1_pair) select_rank<NW, C>(P, smask, S.q1_k + 1, b1);
-  select_rank<NW, C>(P, smask, S.q3_k, a3);
-  if (S.q3_pair) select_rank<NW, C>(P, smask, S.q3_k + 1, b3);
+// 1 / iqr per channel from the packed quartile order statistics (src/chrono.rs:246-252, iqr 0
+// counts as 1); q1v / q3v the quartiles.
+template <int C>
+DEVI void quartiles_from_ranks(const StackDev& S, uint32_t q1a, uint32_t q1b, uint32_t q3a,
+                               uint32_t q3b, float (&q1v)[C], float (&q3v)[C],
+                               float (&iqr_inv)[C]) {
 #pragma unroll
   for (int ch = 0; ch < C; ++ch) {
-    const float q1 = quantile_value(a1[ch], S.q1_pair ? b1[ch] : a1[ch], S.q1_pair != 0, S.q1_frac);
-    const float q3 = quantile_value(a3[ch], S.q3_pair ? b3[ch] : a3[ch], S.q3_pair != 0, S.q3_frac);
+    const uint32_t a1 = (q1a >> (8 * ch)) & 0xFFu, b1 = (q1b >> (8 * ch)) & 0xFFu;
+    const uint32_t a3 = (q3a >> (8 * ch)) & 0xFFu, b3 = (q3b >> (8 * ch)) & 0xFFu;
+    const float q1 = quantile_value(a1, S.q1_pair ? b1 : a1, S.q1_pair != 0, S.q1_frac);
+    const float q3 = quantile_value(a3, S.q3_pair ? b3 : a3, S.q3_pair != 0, S.q3_frac);
     float iqr = __fsub_rn(q3, q1);
     if (iqr == 0.0f) iqr = 1.0f;
     iqr_inv[ch] = __fdiv_rn(1.0f, iqr);
@@ -134,16 +145,18 @@ DEVI void pixel_order_stats(const StackDev& S, int n, Load load, uint32_t& lo3, 
   uint32_t smask[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
-  pixel_median_pair<C, NW>(S, P, smask, lo3, hi3);
+  const bool quart = KIND != kIntKind && !S.thr_abs;
+  uint32_t q1a, q1b, q3a, q3b;
+  pixel_ranks<C, NW, KIND != kIntKind>(S, P, smask, quart, lo3, hi3, q1a, q1b, q3a, q3b);
 #pragma unroll
   for (int ch = 0; ch < C; ++ch) {
     wq[ch] = 0.0f;
     q1v[ch] = 0.0f;
     q3v[ch] = 0.0f;
   }
-  if (KIND != kIntKind && !S.thr_abs) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
+  if (quart) {  // quartiles and w * iqr_inv, src/chrono.rs:246-252
     float iqr_inv[C], q1[C], q3[C];
-    pixel_quartiles<C, NW>(S, P, smask, q1, q3, iqr_inv);
+    quartiles_from_ranks<C>(S, q1a, q1b, q3a, q3b, q1, q3, iqr_inv);
 #pragma unroll
     for (int ch = 0; ch < C; ++ch) {
       wq[ch] = __fmul_rn(S.w[ch], iqr_inv[ch]);
