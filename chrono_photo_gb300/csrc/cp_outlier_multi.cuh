@@ -103,13 +103,30 @@ __global__ void __launch_bounds__(kPxThreads, kMultiMinCtas<NW>)
     int32_t key = -1;
     float dmax = 0.0f;
     int imax = 0;
+    uint32_t carried = 0u;  // the second result of a darker / lighter pair
+    bool have_carried = false;
     for (int s = 0; s < M.count; ++s) {
       const StackDev& T = M.sets[s];
       PxOut r;
       if (T.mode != CP_MODE_OUTLIER) {  // darker / lighter on the same staged rows
-        r.pix = px_simple<C>(T, n, load);
         r.mask = 0u;
         r.warning = false;
+        if (have_carried) {
+          r.pix = carried;
+          have_carried = false;
+        } else if (s + 1 < M.count && M.sets[s + 1].mode != CP_MODE_OUTLIER &&
+                   M.sets[s + 1].mode != T.mode && T.unit_w && T.no_fade &&
+                   M.sets[s + 1].unit_w && M.sets[s + 1].no_fade &&
+                   M.sets[s + 1].wmask == T.wmask) {
+          uint32_t dark, light;
+          px_simple_pair<C>(T, n, load, dark, light);
+          const bool d = T.mode == CP_MODE_DARKER;
+          r.pix = d ? dark : light;
+          carried = d ? light : dark;
+          have_carried = true;
+        } else {
+          r.pix = px_simple<C>(T, n, load);
+        }
       } else {
         uint32_t wbytes = 0;
 #pragma unroll

@@ -313,6 +313,27 @@ DEVI uint32_t px_simple(const StackDev& S, int n, Load load) {
   return outw;
 }
 
+// Darker and lighter of the same weights, both in the integer form (0/1 weights, every fade
+// factor >= 1), in one pass: each sample is loaded and summed once for both extremes.
+template <int C, typename Load>
+DEVI void px_simple_pair(const StackDev& S, int n, Load load, uint32_t& dark, uint32_t& light) {
+  uint32_t ones = 0u;
+#pragma unroll
+  for (int ch = 0; ch < C; ++ch)
+    if ((S.wmask >> ch) & 1u) ones |= 1u << (8 * ch);
+  int32_t lo = 0x7FFFFFFF, hi = -1;
+  dark = light = 0u;
+  for (int i = 0; i < n; ++i) {
+    const uint32_t px = load(i) & (0xFFFFFFFFu >> (32 - 8 * C));
+    const int32_t v = static_cast<int32_t>(__dp4a(px, ones, 0u));
+    const bool dn = v < lo, up = v > hi;
+    lo = dn ? v : lo;
+    dark = dn ? px : dark;
+    hi = up ? v : hi;
+    light = up ? px : light;
+  }
+}
+
 struct PxOut {
   uint32_t pix;   // composite, channel bytes
   uint32_t mask;  // blend mask value of channels 0..2
@@ -493,7 +514,32 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
       binv = __fmul_rn(binv, __fsub_rn(1.0f, bk));
     };
     // outliers in ascending (forward) or descending (backward) sample order
-    if (S.outlier == CP_OUTLIER_FORWARD) {
+    if constexpr (OG == kOgAny) {
+      // the generic epilogue (multi-setting kernel): one loop with one copy of blend_one,
+      // each turn taking the lowest (highest) remaining flag; a smaller instruction footprint
+      // for a kernel that walks every setting kind per tile
+      const bool fwd = S.outlier == CP_OUTLIER_FORWARD;
+      uint32_t m[NW];
+#pragma unroll
+      for (int w = 0; w < NW; ++w) m[w] = pb[w];
+#pragma unroll 1
+      for (int t = 0; t < nout; ++t) {
+        int f = 0;
+        if (fwd) {
+#pragma unroll
+          for (int w = NW - 1; w >= 0; --w)
+            if (m[w]) f = 32 * w + __ffs(m[w]) - 1;
+        } else {
+#pragma unroll
+          for (int w = 0; w < NW; ++w)
+            if (m[w]) f = 32 * w + 31 - __clz(m[w]);
+        }
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+          if (w == (f >> 5)) m[w] &= ~(1u << (f & 31));
+        blend_one(f);
+      }
+    } else if (S.outlier == CP_OUTLIER_FORWARD) {
 #pragma unroll
       for (int w = 0; w < NW; ++w) {
         uint32_t m = pb[w];

@@ -190,3 +190,19 @@ def test_benchmark_step_is_one_launch(ctx):
     device_multi(ctx, frames, ps + [other])
     l2, m2, s2 = launch_counts(ctx)
     assert (l2 - l1, m2 - m1, s2 - s1) == (2, 1, 6)
+
+
+@pytest.mark.parametrize("order", [("lighter", "darker"), ("darker", "lighter")])
+def test_darker_lighter_pair(ctx, order):
+    """Darker and lighter next to each other (0/1 weights, no fade) fold in one pass over the
+    samples, whichever comes first; ties keep the earliest frame."""
+    rng = np.random.default_rng(16)
+    frames = cases.random_stack(rng, 40, 24, 48, 3, n_spots=3)
+    frames[7] = frames[3]  # equal sums: the earlier frame wins
+    kws = [dict(mode="outlier", threshold="abs/0.05/0.2", outlier="extreme",
+                background="first")] + [dict(mode=m) for m in order]
+    ps = [cases.params(**kw) for kw in kws]
+    for kw, p, (o, b, wn) in zip(kws, ps, device_multi(ctx, frames, ps)):
+        ref = device_single(ctx, frames, p)
+        assert np.array_equal(o, ref[0]), kw
+        cases.assert_close_u8(o, oracle.composite(frames, p)[0], what=str(kw))
