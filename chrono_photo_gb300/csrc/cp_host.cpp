@@ -363,6 +363,8 @@ int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream) {
 
 namespace {
 
+}  // namespace
+
 // The pixel-thread kernels take the stack (RGB, aligned rows, no crop, integer or paired f32
 // distances); the multi-setting kernel takes those same stacks.
 bool px_eligible(cp_ctx* ctx, const StackDev& d) {
@@ -370,6 +372,8 @@ bool px_eligible(cp_ctx* ctx, const StackDev& d) {
          (d.fast_int || d.pair_f32) && px_smem_bytes(d.n, false) <= ctx->max_smem &&
          (d.nw == 1 || d.nw == 2 || d.nw == 4);
 }
+
+namespace {
 
 // Darker / lighter settings the multi-setting kernel folds on its staged rows: RGB, rows
 // starting 16-byte aligned, no crop.

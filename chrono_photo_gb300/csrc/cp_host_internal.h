@@ -93,6 +93,9 @@ int fade_lut(const cp_fade* f, int32_t n, int32_t frame_offset, float* out);
 int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
                   const uint8_t* const* dev_frames, StackDev* d);
 int launch_single(cp_ctx* ctx, const StackDev& d, cudaStream_t stream);
+// The stack takes the pixel-thread kernels (RGB, aligned rows, no crop, integer or paired f32
+// distances, shared memory for its frames).
+bool px_eligible(cp_ctx* ctx, const StackDev& d);
 inline void count_launches(cp_ctx* ctx, uint64_t n) { ctx->n_launches += n; }
 // Several settings of one stack (and band): the pixel-kernel settings sharing their order
 // statistics in multi-setting launches of up to kMultiMax, the rest one by one.

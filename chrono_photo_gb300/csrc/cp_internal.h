@@ -173,6 +173,8 @@ inline int single_variant(const StackDev& s) {
 // aligned frame rows and no crop, distance kind 1 (integer) or 2 (paired f32). A CTA of
 // kPxThreads threads; phase A's order statistics reach the pixel threads through PxAux.
 constexpr int kPxThreads = 128;
+// CTAs per SM the batch routing assumes for the pixel-thread kernel (its 64-frame residency)
+constexpr int kPxAloneCtas = 7;
 struct PxAux {
   uint32_t lo[4][32], hi[4][32];  // word w of column t; word 3 is zero (funnel padding)
   float wq[12][32];               // rel: w * iqr_inv of byte position q of column t

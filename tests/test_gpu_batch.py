@@ -156,3 +156,30 @@ def test_video_windows_match_oracle(ctx):
                 cases.assert_close_u8(ctx.download(blends[k], (36, 50, 3)), ref[1], what="window %d" % k)
     finally:
         ds.free()
+
+
+def test_big_stacks_leave_the_batch(ctx):
+    """A stack that fills the GPU alone (16 x 480x640: 2400 tiles of 128 pixels) runs on the
+    pixel-thread kernel by itself, the small ones in the batched launch; every stack still
+    matches the oracle and its own warnings."""
+    rng = np.random.default_rng(21)
+    big = cases.random_stack(rng, 16, 480, 640, 3, n_spots=6)
+    small = [cases.random_stack(rng, n, h, w, 3, n_spots=3)
+             for n, h, w in ((20, 40, 64), (33, 24, 48), (9, 30, 70))]
+    kws = [dict(mode="outlier", threshold="abs/0.05/0.2", outlier="extreme", background="first"),
+           dict(mode="outlier", threshold="rel/2/4", outlier="average", background="first"),
+           dict(mode="outlier", threshold="abs/0.05/0.2", outlier="forward", background="median"),
+           dict(mode="outlier", threshold="abs/0.04", outlier="last", background="average")]
+    items = [(big, kws[0], 0)] + [(f, kw, 0) for f, kw in zip(small, kws[1:])]
+    counts0 = ct.c_uint64()
+    ctx.check(_abi.lib().cp_ctx_launch_counts(ctx.handle, ct.byref(counts0), None, None))
+    got = run_batch(ctx, items)
+    counts1 = ct.c_uint64()
+    ctx.check(_abi.lib().cp_ctx_launch_counts(ctx.handle, ct.byref(counts1), None, None))
+    assert counts1.value - counts0.value >= 2  # the big stack alone, then the batch
+    for (frames, kw, off), (o, b, wn) in zip(items, got):
+        p = cases.params(**kw)
+        ref = oracle.composite(frames, p, threads=8)
+        cases.assert_close_u8(o, ref[0], what="%s composite" % kw)
+        cases.assert_close_u8(b, ref[1], what="%s blend" % kw)
+        assert wn == ref[2]
