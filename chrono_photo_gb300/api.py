@@ -565,6 +565,17 @@ def save_image(path, image, quality=95, threads=0, context=None):
         raise ValueError("output format by extension: .png, .jpg or .jpeg")
 
 
+def sample_indices(n, count, seed=0x5EED):
+    """Seeded sub-sample of min(count, n) sorted distinct positions of n frames
+    (cp_sample_indices; the reference draws them unseeded, src/chrono.rs:153-158)."""
+    out = np.zeros(max(int(n), 1), np.int32)
+    got = ct.c_int32(0)
+    _check(None, lib().cp_sample_indices(int(n), int(count), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                         out.ctypes.data_as(_abi.I32P), ct.byref(got)),
+           "cp_sample_indices")
+    return [int(v) for v in out[:got.value]]
+
+
 def video_windows(image_count, video_in, video_out=(None, None, 1)):
     """chrono-video windows of src/main.rs:230-286: list of (output frame, indices)."""
     (a, b, s), (c, d, t) = video_in, video_out
