@@ -35,8 +35,8 @@ BATCH_VARIANTS = [(3, k, g, 1) for k in (1, 2) for g in (1, 2, 3)]
 # cp_kernels_px.cu compiled once per pixel-thread kernel family (distance kind, outlier
 # group, background): the CP_PX_VARIANTS list of cp_internal.h
 PX_VARIANTS = [(k, g, b) for k in (1, 2) for b in (1, 0) for g in (1, 2, 3)]
-CPP_SOURCES = ["cp_host.cpp", "cp_stage.cpp", "cp_batch.cpp", "cp_shake_host.cpp",
-               "cp_server.cpp", "cp_ingest.cpp", "cp_png_write.cpp", "cp_tune.cpp",
+CPP_SOURCES = ["cp_host.cpp", "cp_prepare.cpp", "cp_memory.cpp", "cp_stage.cpp", "cp_batch.cpp",
+               "cp_shake_host.cpp", "cp_server.cpp", "cp_ingest.cpp", "cp_png_write.cpp", "cp_tune.cpp",
                "cp_jpeg.cpp", "cp_jpeg_write.cpp"]
 HEADERS = ["cp_internal.h", "cp_host_internal.h", "cp_tile.cuh", "cp_png.h", "cp_pixel.cuh",
            "cp_outlier_px.cuh", "cp_outlier_multi.cuh", "cp_io.h"]

@@ -260,6 +260,16 @@ int admit(cp_server* srv, Job* j) {
 void release(cp_server* srv, Job* j) {
   for (Frame* f : j->frames)
     if (f) f->refs -= 1;
+  if (!j->private_frames.empty() && !j->staged) {
+    // admission failed before it joined the second copy stream into the first: uploads of
+    // this job may still be queued there, and the frees below (on the first stream) must
+    // follow them
+    cudaEvent_t join = nullptr;
+    cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    cudaEventRecord(join, srv->h2d2);
+    cudaStreamWaitEvent(srv->h2d, join, 0);
+    cudaEventDestroy(join);
+  }
   for (Frame* f : j->private_frames) {
     cudaEventDestroy(f->ready);
     pool_free(srv->ctx, f->dev, f->bytes, srv->h2d);
