@@ -62,8 +62,13 @@ DEVI void pixel_planes(int n, Load load, uint32_t (&P)[C][8][NW]) {
 #pragma unroll
     for (int g = 0; g < 4; ++g) {
       const int f0 = blk * 32 + g * 8;
+      if (f0 + 8 <= n) {  // a whole group: no per-sample bound test
 #pragma unroll
-      for (int r = 0; r < 8; ++r) a[g][r] = (f0 + r < n) ? load(f0 + r) : 0u;
+        for (int r = 0; r < 8; ++r) a[g][r] = load(f0 + r);
+      } else {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) a[g][r] = (f0 + r < n) ? load(f0 + r) : 0u;
+      }
       transpose8(a[g]);
     }
 #pragma unroll
@@ -180,24 +185,50 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
   key = st.nh > 0 ? -1 : 255;
   dmax = 0.0f;
   imax = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) pb[w] = 0u;
+  // Full 32-sample words run as two straight-line chunks of 16 samples (immediate shared
+  // memory offsets, no per-sample bound test); a partial last word takes the general loop.
+  // The word loop is not unrolled (one copy of each chunk): its flag word reaches pb[w]
+  // through uniform selects.
   if (KIND == kIntKind || ((KIND == kAnyKind || KIND == kPxKind) && S.fast_int)) {
     const int32_t thr1 = S.thr_int[st.nh] - 1;
-#pragma unroll
+    // thr1 - d = (thr1 - klo.khi) + v.klo + v.khi - v.v, accumulated by the dp4a chain
+    const uint32_t base = static_cast<uint32_t>(thr1) - __dp4a(st.klo, st.khi, 0u);
+#pragma unroll 1
     for (int blk = 0; blk < NW; ++blk) {
       // flags enter at bit 0 and move up (a funnel shift takes the sign of thr - 1 - d:
       // set iff d >= thr); one bit reversal puts sample i at bit i
       uint32_t ob = 0u;
-      const int i0 = blk * 32, iend = min(n, i0 + 32);
+      const int i0 = blk * 32, cnt = min(n - i0, 32);
+      if (cnt == 32) {
+#pragma unroll 1
+        for (int h = i0; h < i0 + 32; h += 16) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const uint32_t v = load(h + j) & wbytes;
+            const uint32_t t = __dp4a(v, st.khi, __dp4a(v, st.klo, base)) - __dp4a(v, v, 0u);
+            ob = __funnelshift_l(t, ob, 1);
+            if (kKeepMax<OG>) {
+              const int32_t kv = ((thr1 - static_cast<int32_t>(t)) << 8) + 255 - (h + j);
+              key = kv > key ? kv : key;
+            }
+          }
+        }
+      } else {
 #pragma unroll 4
-      for (int i = i0; i < iend; ++i) {
-        const int32_t d = static_cast<int32_t>(dist_int(load(i), wbytes, st.klo, st.khi));
-        ob = __funnelshift_l(static_cast<uint32_t>(thr1 - d), ob, 1);
-        if (kKeepMax<OG>) {
-          const int32_t kv = (d << 8) + 255 - i;
-          key = kv > key ? kv : key;
+        for (int i = i0; i < i0 + cnt; ++i) {
+          const int32_t d = static_cast<int32_t>(dist_int(load(i), wbytes, st.klo, st.khi));
+          ob = __funnelshift_l(static_cast<uint32_t>(thr1 - d), ob, 1);
+          if (kKeepMax<OG>) {
+            const int32_t kv = (d << 8) + 255 - i;
+            key = kv > key ? kv : key;
+          }
         }
       }
-      pb[blk] = iend > i0 ? __brev(ob) >> (32 - (iend - i0)) : 0u;
+      ob = cnt > 0 ? __brev(ob) >> (32 - cnt) : 0u;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) pb[w] = w == blk ? ob : pb[w];
     }
   } else if (KIND == kF32Kind || KIND == kPxKind || (KIND == kAnyKind && S.pair_f32)) {
     // two samples per instruction in float2 lanes, every term on (median - p) / 2: the
@@ -213,11 +244,51 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
       wq2[ch] = make_float2(st.wi[ch], st.wi[ch]);
     }
     const float thr4 = __fmul_rn(S.thr_sq, 0.25f);
+    // every channel of two samples; a weight-0 channel adds +0 (w * iqr_inv = 0 and the
+    // median term finite), which leaves the non-negative sum unchanged
+    auto pair_dist = [&](uint32_t p0, uint32_t p1) -> float2 {
+      float2 dq = make_float2(0.0f, 0.0f);
 #pragma unroll
+      for (int ch = 0; ch < C; ++ch) {
+        const uint32_t sel = 0x7604u | (static_cast<uint32_t>(ch) << 4);
+        const float2 nv = make_float2(__uint_as_float(__byte_perm(p0, 0xC6800000u, sel)),
+                                      __uint_as_float(__byte_perm(p1, 0xC6800000u, sel)));
+        const float2 tt = mul2_rn(wq2[ch], add2_rn(mq[ch], nv));
+        const float2 sq = mul2_rn(tt, tt);
+        dq.x = __fadd_rn(dq.x, sq.x);
+        dq.y = __fadd_rn(dq.y, sq.y);
+      }
+      return dq;
+    };
+#pragma unroll 1
     for (int blk = 0; blk < NW; ++blk) {
       uint32_t ob = 0u;
-      const int iend = min(n, blk * 32 + 32);
-      for (int i = blk * 32; i < iend; i += 2) {
+      const int i0 = blk * 32, iend = min(n, i0 + 32);
+      if (iend - i0 == 32) {
+        // the sign of dq - thr4 is 0 exactly when dq >= thr4 (equal: +0; both finite and
+        // non-negative): sign bits of non-outliers enter at bit 0 and move up
+        uint32_t nb = 0u;
+#pragma unroll 1
+        for (int h = i0; h < i0 + 32; h += 16) {
+#pragma unroll
+          for (int j = 0; j < 16; j += 2) {
+            const int i = h + j;
+            const float2 dq = pair_dist(load(i), load(i + 1));
+            nb = __funnelshift_l(__float_as_uint(__fsub_rn(dq.x, thr4)), nb, 1);
+            nb = __funnelshift_l(__float_as_uint(__fsub_rn(dq.y, thr4)), nb, 1);
+            if (kKeepMax<OG>) {
+              const bool u0 = dq.x >= thr4 && dq.x > dmax;
+              dmax = u0 ? dq.x : dmax;
+              imax = u0 ? i : imax;
+              const bool u1 = dq.y >= thr4 && dq.y > dmax;
+              dmax = u1 ? dq.y : dmax;
+              imax = u1 ? i + 1 : imax;
+            }
+          }
+        }
+        ob = ~__brev(nb);
+      }
+      for (int i = i0; i < iend && iend - i0 < 32; i += 2) {
         const uint32_t p0 = load(i);
         const uint32_t p1 = i + 1 < iend ? load(i + 1) : p0;
         float2 dq = make_float2(0.0f, 0.0f);
@@ -249,7 +320,8 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
           }
         }
       }
-      pb[blk] = ob;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) pb[w] = w == blk ? ob : pb[w];
     }
     dmax = __fmul_rn(dmax, 4.0f);  // scaled back exactly
   } else {
@@ -467,7 +539,12 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
   const bool single_group = og_is<OG>(S, kOgSingle);
   const bool blend_group = og_is<OG>(S, kOgBlend);
   const bool extreme = single_group && S.outlier == CP_OUTLIER_EXTREME;
-  const bool multi = nout > 1 && !single_group;
+  // the average group takes every outlier count through the averaging branch: with one
+  // outlier its sums are that sample's bytes and its distance (divided by 1, exact), and the
+  // fade is taken at that sample, as the single-sample branch does; one branch instead of
+  // two for warps that mix single- and multi-outlier pixels
+  const bool avg_group = og_is<OG>(S, kOgAverage);
+  const bool multi = !single_group && (nout > 1 || avg_group);
   if (!multi) {
     int si;
     float dsq = 0.0f;
@@ -565,8 +642,9 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
     for (int ch = 0; ch < C; ++ch) pix |= sat_u8(rround(pf[ch])) << (8 * ch);
     mask = sat_u8(rround(__fmul_rn(__fsub_rn(1.0f, binv), 255.0f)));
     chosen = -2;
-  } else {  // average of several outliers, src/chrono.rs:429-468
+  } else {  // average of the outliers, src/chrono.rs:429-468 (one or none: :377-428)
     // channel sums in 16-bit lanes (n * 255 < 2^16): even bytes, odd bytes
+    const int si = first_set<NW>(pb);  // the outlier, when there is one
     uint32_t se = 0u, so = 0u;
     float mdist = 0.0f;
 #pragma unroll
@@ -588,11 +666,14 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
       const uint32_t os = ((ch & 1) ? so : se) >> (16 * (ch >> 1)) & 0xFFFFu;
       sample |= sat_u8(rround(__fdiv_rn(static_cast<float>(os), kf))) << (8 * ch);
     }
-    // the fade of an averaged outlier is taken at sample 0 (src/chrono.rs:467)
-    blend = __fmul_rn(S.fade[0], blend_value(S, __fdiv_rn(mdist, kf)));
+    // the fade of an averaged outlier is taken at sample 0 (src/chrono.rs:467), that of a
+    // single one at its own sample; no outlier: no blend (the sums divided by 0 are unused)
+    const float bk =
+        __fmul_rn(S.fade[nout == 1 ? si : 0], blend_value(S, __fdiv_rn(mdist, kf)));
+    blend = nout == 0 ? 0.0f : bk;
     pix = blend_into_u8<C>(pix, sample, blend);
     mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
-    chosen = 0;
+    chosen = nout == 0 ? -1 : (nout == 1 ? si : 0);
   }
   r.pix = pix;
   r.mask = mask;

@@ -97,3 +97,62 @@ def test_static_batch_limit(ctx):
     pa = (_abi.Params * 65)()
     outs = (ct.c_void_p * 65)()
     assert _abi.lib().cp_composite_batch_static(st, pa, 65, outs, None, None, None) == _abi.CP_ERR_LIMIT
+
+
+def test_static_batch_replays_from_a_captured_graph(ctx):
+    """The call reads no host memory after it returns (the descriptors travel as kernel
+    parameters), so it can be captured into a CUDA graph: two replays of the captured call
+    give the oracle's composites."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    specs = [(12, 24, 40, dict(mode="outlier", outlier="average", background="first")),
+             (36, 16, 72, dict(mode="outlier", threshold="rel/2/5", outlier="backward",
+                               background="median"))]
+    n_st = len(specs)
+    ptrs, keep, shapes, oracle_out = [], [], [], []
+    try:
+        stacks = (_abi.Stack * n_st)()
+        params = (_abi.Params * n_st)()
+        outs = (ct.c_void_p * n_st)()
+        blends = (ct.c_void_p * n_st)()
+        for i, (n, h, w, kw) in enumerate(specs):
+            frames = cases.random_stack(rng, n, h, w, 3, n_spots=4)
+            base = ctx.upload(frames)
+            ptrs.append(base)
+            stacks[i] = _abi.Stack(n=n, width=w, height=h, channels=3, base=base,
+                                   frame_stride=h * w * 3, frame_offset=0)
+            params[i] = cg.make_params(keep=keep, **kw)
+            oracle_out.append(oracle.composite(frames, params[i], frame_offset=0))
+            outs[i] = ctx.alloc(h * w * 3)
+            blends[i] = ctx.alloc(h * w * 3)
+            ptrs += [outs[i], blends[i]]
+            shapes.append((h, w, 3))
+        warn = ctx.alloc(8 * n_st)
+        ptrs.append(warn)
+        s = torch.cuda.Stream()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            rc = _abi.lib().cp_composite_batch_static(stacks, params, n_st, outs, blends, warn,
+                                                      ct.c_void_p(s.cuda_stream))
+        assert rc == _abi.CP_OK
+        for replay in range(2):
+            ctx.upload(np.zeros(n_st, np.uint64), warn)
+            for i, shp in enumerate(shapes):
+                ctx.upload(np.full(shp, 77, np.uint8), outs[i])
+            g.replay()
+            s.synchronize()
+            status = ct.c_int32(-99)
+            assert _abi.lib().cp_composite_batch_static_status(
+                ct.byref(status), ct.c_void_p(s.cuda_stream)) == 0
+            assert status.value == _abi.CP_OK
+            for i, shp in enumerate(shapes):
+                cases.assert_close_u8(ctx.download(outs[i], shp), oracle_out[i][0],
+                                      what="replay %d composite %d" % (replay, i))
+                cases.assert_close_u8(ctx.download(blends[i], shp), oracle_out[i][1],
+                                      what="replay %d blend %d" % (replay, i))
+            assert [int(x) for x in ctx.download(warn, (n_st,), np.uint64)] == \
+                [o[2] for o in oracle_out]
+        del g
+    finally:
+        for p in ptrs:
+            ctx.free(p)
