@@ -85,18 +85,36 @@ DEVI void pixel_planes(int n, Load load, uint32_t (&P)[C][8][NW]) {
   }
 }
 
-// The median pair and, with QUART, the quartile pairs of one pixel through ONE copy of the
-// selection code: a runtime loop over the needed ranks (med_k, med_k + 1 if paired, q1_k,
-// q1_k + 1, q3_k, q3_k + 1 if paired) instead of one inlined selection per rank (six for rel
-// thresholds, each some 300 instructions: their code footprint stalled instruction fetch).
-// Results are packed per rank (channel byte ch at bits 8ch) and kept in named registers
-// through uniform selects, so no array is indexed at run time.
+// The median pair and, with QUART, the quartile pairs of one pixel. With QUART the ranks go
+// through ONE copy of the selection code: a runtime loop over the needed ranks (med_k,
+// med_k + 1 if paired, q1_k, q1_k + 1, q3_k, q3_k + 1 if paired) instead of one inlined
+// selection per rank (six for rel thresholds, each some 300 instructions: their code
+// footprint stalled instruction fetch). Without QUART the median pair's two selections are
+// straight-line code. Results are packed per rank (channel byte ch at bits 8ch) and kept in
+// named registers through uniform selects, so no array is indexed at run time.
 // quart: the quartiles are wanted (QUART compiles them in).
 template <int C, int NW, bool QUART>
 DEVI void pixel_ranks(const StackDev& S, const uint32_t (&P)[C][8][NW],
                       const uint32_t (&smask)[NW], bool quart, uint32_t& lo3, uint32_t& hi3,
                       uint32_t& q1a, uint32_t& q1b, uint32_t& q3a, uint32_t& q3b) {
   lo3 = hi3 = q1a = q1b = q3a = q3b = 0u;
+  auto pack = [](const uint32_t (&v)[C]) {
+    uint32_t packed = 0u;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) packed |= v[ch] << (8 * ch);
+    return packed;
+  };
+  if constexpr (!QUART) {  // the median pair alone: two straight-line selections
+    uint32_t v[C];
+    select_rank<NW, C>(P, smask, S.med_k, v);
+    lo3 = pack(v);
+    hi3 = lo3;
+    if (S.med_pair) {
+      select_rank<NW, C>(P, smask, S.med_k + 1, v);
+      hi3 = pack(v);
+    }
+    return;
+  }
   const int nrank = QUART && quart ? 6 : 2;
 #pragma unroll 1
   for (int j = 0; j < nrank; ++j) {
@@ -106,9 +124,7 @@ DEVI void pixel_ranks(const StackDev& S, const uint32_t (&P)[C][8][NW],
     const int k = j < 2 ? S.med_k + j : (j < 4 ? S.q1_k + j - 2 : S.q3_k + j - 4);
     uint32_t v[C];
     select_rank<NW, C>(P, smask, k, v);
-    uint32_t packed = 0u;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) packed |= v[ch] << (8 * ch);
+    const uint32_t packed = pack(v);
     lo3 = j == 0 ? packed : lo3;
     hi3 = j == 1 ? packed : hi3;
     q1a = j == 2 ? packed : q1a;
