@@ -180,9 +180,14 @@ struct PxAux {
   float wq[12][32];               // rel: w * iqr_inv of byte position q of column t
   uint32_t out[3][32], blend[3][32];
 };
-// header + one or two (double-buffered) stage buffers of n rows + PxAux
+// Stage rows of the pixel-thread kernels: n padded to whole 32-sample words. The copies fill
+// rows 0..n-1; the kernels zero the rest once, so that the bit planes load every sample of
+// a word without bound tests (the sample mask leaves the padding out of every statistic).
+inline int px_stage_rows(int n) { return 32 * nw_for(n); }
+// header + one or two (double-buffered) stage buffers of the padded rows + PxAux
 inline int px_smem_bytes(int n, bool db) {
-  return kSmemHeader + (db ? 2 : 1) * n * row_pitch_host(3) + static_cast<int>(sizeof(PxAux));
+  return kSmemHeader + (db ? 2 : 1) * px_stage_rows(n) * row_pitch_host(3) +
+         static_cast<int>(sizeof(PxAux));
 }
 // Several outlier settings of one stack in one pass (k_outlier_multi, cp_outlier_multi.cuh):
 // the settings' descriptors, kernel parameters; sets[0] also gives the frames, geometry and

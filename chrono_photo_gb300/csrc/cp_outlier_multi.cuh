@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kPxThreads, kMultiMinCtas<NW>)
   uintptr_t* fbase = reinterpret_cast<uintptr_t*>(smem + 256);
   uint8_t* buf = smem + kSmemHeader;
   const int n = S.n;
-  MultiAux& A = *reinterpret_cast<MultiAux*>(buf + n * kPitch<C>);
+  MultiAux& A = *reinterpret_cast<MultiAux*>(buf + 32 * NW * kPitch<C>);  // padded rows
   const int warp = static_cast<int>(threadIdx.x) >> 5;
   const int lane = static_cast<int>(threadIdx.x) & 31;
   if (threadIdx.x == 0) {
@@ -51,6 +51,9 @@ __global__ void __launch_bounds__(kPxThreads, kMultiMinCtas<NW>)
   }
   for (int f = threadIdx.x; f < n; f += kPxThreads)
     fbase[f] = reinterpret_cast<uintptr_t>(S.frames[f]);
+  // the padding rows n..32*NW-1 stay zero: the copies write rows 0..n-1 only
+  for (int i = threadIdx.x; i < (32 * NW - n) * (kPitch<C> / 4); i += kPxThreads)
+    reinterpret_cast<uint32_t*>(buf + n * kPitch<C>)[i] = 0u;
   __syncthreads();
   uint32_t phase = 0;
   const int stride = static_cast<int>(gridDim.x);
@@ -83,7 +86,7 @@ __global__ void __launch_bounds__(kPxThreads, kMultiMinCtas<NW>)
     float iqr_inv[C];
     {
       uint32_t P[C][8][NW];
-      pixel_planes<C, NW>(n, load, P);
+      pixel_planes<C, NW>(load, P);
       uint32_t smask[NW];
 #pragma unroll
       for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];

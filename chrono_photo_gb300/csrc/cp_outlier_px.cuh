@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB, PA>))
   uintptr_t* fbase = reinterpret_cast<uintptr_t*>(smem + 256);
   uint8_t* stage0 = smem + kSmemHeader;
   const int n = S.n;
-  const int stage_bytes = n * kPitch<C>;
+  const int stage_bytes = 32 * NW * kPitch<C>;  // rows padded to whole words (px_stage_rows)
   PxAux& A = *reinterpret_cast<PxAux*>(stage0 + (DB ? 2 : 1) * stage_bytes);
   const int warp = static_cast<int>(threadIdx.x) >> 5;
   const int lane = static_cast<int>(threadIdx.x) & 31;
@@ -54,6 +54,11 @@ __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB, PA>))
   }
   for (int f = threadIdx.x; f < n; f += kPxThreads)
     fbase[f] = reinterpret_cast<uintptr_t>(S.frames[f]);
+  // the padding rows n..32*NW-1 stay zero: the copies write rows 0..n-1 only
+  for (int b = 0; b < (DB ? 2 : 1); ++b) {
+    uint32_t* z = reinterpret_cast<uint32_t*>(stage0 + b * stage_bytes + n * kPitch<C>);
+    for (int i = threadIdx.x; i < (32 * NW - n) * (kPitch<C> / 4); i += kPxThreads) z[i] = 0u;
+  }
   if (threadIdx.x < 32) {
     A.lo[3][lane] = 0u;
     A.hi[3][lane] = 0u;
@@ -130,7 +135,7 @@ __global__ void __launch_bounds__(kPxThreads, (kPxMinCtas<NW, DB, PA>))
       float wq3[C];
       if (PA == 2) {
         float q1v[C], q3v[C];
-        pixel_order_stats<C, NW, KIND>(S, n, load, lo3, hi3, wq3, q1v, q3v);
+        pixel_order_stats<C, NW, KIND>(S, load, lo3, hi3, wq3, q1v, q3v);
         if (pin < g.npx && (S.dbg_q1 || S.dbg_q3)) {
 #pragma unroll
           for (int ch = 0; ch < C; ++ch) {

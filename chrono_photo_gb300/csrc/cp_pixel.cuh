@@ -54,21 +54,17 @@ DEVI PxStat<C> px_stat(const StackDev& S, uint32_t lo3, uint32_t hi3, const floa
 
 // Bit planes of one pixel's samples: P[ch][r][blk] bit i = bit r of channel byte ch of sample
 // 32*blk + i (8x8 bit transposes of 8 samples, then a 4x4 byte transpose of 4 groups).
+// Every sample 0..32*NW-1 is loaded: the stage rows past the stack's n are zero (the sample
+// mask keeps them out of the selections), so the loads need no bound test.
 template <int C, int NW, typename Load>
-DEVI void pixel_planes(int n, Load load, uint32_t (&P)[C][8][NW]) {
+DEVI void pixel_planes(Load load, uint32_t (&P)[C][8][NW]) {
 #pragma unroll
   for (int blk = 0; blk < NW; ++blk) {
     uint32_t a[4][8];
 #pragma unroll
     for (int g = 0; g < 4; ++g) {
-      const int f0 = blk * 32 + g * 8;
-      if (f0 + 8 <= n) {  // a whole group: no per-sample bound test
 #pragma unroll
-        for (int r = 0; r < 8; ++r) a[g][r] = load(f0 + r);
-      } else {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) a[g][r] = (f0 + r < n) ? load(f0 + r) : 0u;
-      }
+      for (int r = 0; r < 8; ++r) a[g][r] = load(blk * 32 + g * 8 + r);
       transpose8(a[g]);
     }
 #pragma unroll
@@ -85,36 +81,18 @@ DEVI void pixel_planes(int n, Load load, uint32_t (&P)[C][8][NW]) {
   }
 }
 
-// The median pair and, with QUART, the quartile pairs of one pixel. With QUART the ranks go
-// through ONE copy of the selection code: a runtime loop over the needed ranks (med_k,
-// med_k + 1 if paired, q1_k, q1_k + 1, q3_k, q3_k + 1 if paired) instead of one inlined
-// selection per rank (six for rel thresholds, each some 300 instructions: their code
-// footprint stalled instruction fetch). Without QUART the median pair's two selections are
-// straight-line code. Results are packed per rank (channel byte ch at bits 8ch) and kept in
-// named registers through uniform selects, so no array is indexed at run time.
+// The median pair and, with QUART, the quartile pairs of one pixel through ONE copy of the
+// selection code: a runtime loop over the needed ranks (med_k, med_k + 1 if paired, q1_k,
+// q1_k + 1, q3_k, q3_k + 1 if paired) instead of one inlined selection per rank (six for rel
+// thresholds, each some 300 instructions: their code footprint stalled instruction fetch).
+// Results are packed per rank (channel byte ch at bits 8ch) and kept in named registers
+// through uniform selects, so no array is indexed at run time.
 // quart: the quartiles are wanted (QUART compiles them in).
 template <int C, int NW, bool QUART>
 DEVI void pixel_ranks(const StackDev& S, const uint32_t (&P)[C][8][NW],
                       const uint32_t (&smask)[NW], bool quart, uint32_t& lo3, uint32_t& hi3,
                       uint32_t& q1a, uint32_t& q1b, uint32_t& q3a, uint32_t& q3b) {
   lo3 = hi3 = q1a = q1b = q3a = q3b = 0u;
-  auto pack = [](const uint32_t (&v)[C]) {
-    uint32_t packed = 0u;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) packed |= v[ch] << (8 * ch);
-    return packed;
-  };
-  if constexpr (!QUART) {  // the median pair alone: two straight-line selections
-    uint32_t v[C];
-    select_rank<NW, C>(P, smask, S.med_k, v);
-    lo3 = pack(v);
-    hi3 = lo3;
-    if (S.med_pair) {
-      select_rank<NW, C>(P, smask, S.med_k + 1, v);
-      hi3 = pack(v);
-    }
-    return;
-  }
   const int nrank = QUART && quart ? 6 : 2;
 #pragma unroll 1
   for (int j = 0; j < nrank; ++j) {
@@ -124,7 +102,9 @@ DEVI void pixel_ranks(const StackDev& S, const uint32_t (&P)[C][8][NW],
     const int k = j < 2 ? S.med_k + j : (j < 4 ? S.q1_k + j - 2 : S.q3_k + j - 4);
     uint32_t v[C];
     select_rank<NW, C>(P, smask, k, v);
-    const uint32_t packed = pack(v);
+    uint32_t packed = 0u;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) packed |= v[ch] << (8 * ch);
     lo3 = j == 0 ? packed : lo3;
     hi3 = j == 1 ? packed : hi3;
     q1a = j == 2 ? packed : q1a;
@@ -159,10 +139,10 @@ DEVI void quartiles_from_ranks(const StackDev& S, uint32_t q1a, uint32_t q1b, ui
 // median pair and, for rel thresholds, the quartiles (src/chrono.rs:220-255). lo3 / hi3 as
 // for px_stat; wq = w * iqr_inv; q1v / q3v the quartiles (debug outputs).
 template <int C, int NW, int KIND, typename Load>
-DEVI void pixel_order_stats(const StackDev& S, int n, Load load, uint32_t& lo3, uint32_t& hi3,
+DEVI void pixel_order_stats(const StackDev& S, Load load, uint32_t& lo3, uint32_t& hi3,
                             float (&wq)[C], float (&q1v)[C], float (&q3v)[C]) {
   uint32_t P[C][8][NW];
-  pixel_planes<C, NW>(n, load, P);
+  pixel_planes<C, NW>(load, P);
   uint32_t smask[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) smask[w] = S.sample_mask[w];
@@ -203,48 +183,40 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
   imax = 0;
 #pragma unroll
   for (int w = 0; w < NW; ++w) pb[w] = 0u;
-  // Full 32-sample words run as two straight-line chunks of 16 samples (immediate shared
-  // memory offsets, no per-sample bound test); a partial last word takes the general loop.
-  // The word loop is not unrolled (one copy of each chunk): its flag word reaches pb[w]
-  // through uniform selects.
+  // Each 32-sample word runs in straight-line chunks of 8 samples (immediate shared-memory
+  // offsets, no per-sample bound test), then a loop over the samples left. The word loop is
+  // not unrolled (one copy of the chunk): its flag word reaches pb[w] through uniform selects.
   if (KIND == kIntKind || ((KIND == kAnyKind || KIND == kPxKind) && S.fast_int)) {
     const int32_t thr1 = S.thr_int[st.nh] - 1;
     // thr1 - d = (thr1 - klo.khi) + v.klo + v.khi - v.v, accumulated by the dp4a chain
     const uint32_t base = static_cast<uint32_t>(thr1) - __dp4a(st.klo, st.khi, 0u);
+    // flags enter at bit 0 and move up (a funnel shift takes the sign of thr - 1 - d: set
+    // iff d >= thr); one bit reversal per word puts sample i at bit i
+    uint32_t ob;
+    auto sample = [&](int i) {
+      const uint32_t v = load(i) & wbytes;
+      const uint32_t t = __dp4a(v, st.khi, __dp4a(v, st.klo, base)) - __dp4a(v, v, 0u);
+      ob = __funnelshift_l(t, ob, 1);
+      if (kKeepMax<OG>) {
+        const int32_t kv = ((thr1 - static_cast<int32_t>(t)) << 8) + 255 - i;
+        key = kv > key ? kv : key;
+      }
+    };
 #pragma unroll 1
     for (int blk = 0; blk < NW; ++blk) {
-      // flags enter at bit 0 and move up (a funnel shift takes the sign of thr - 1 - d:
-      // set iff d >= thr); one bit reversal puts sample i at bit i
-      uint32_t ob = 0u;
-      const int i0 = blk * 32, cnt = min(n - i0, 32);
-      if (cnt == 32) {
+      const int i0 = blk * 32, iend = min(n, i0 + 32);
+      ob = 0u;
+      int i = i0;
 #pragma unroll 1
-        for (int h = i0; h < i0 + 32; h += 16) {
+      for (; i + 8 <= iend; i += 8) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const uint32_t v = load(h + j) & wbytes;
-            const uint32_t t = __dp4a(v, st.khi, __dp4a(v, st.klo, base)) - __dp4a(v, v, 0u);
-            ob = __funnelshift_l(t, ob, 1);
-            if (kKeepMax<OG>) {
-              const int32_t kv = ((thr1 - static_cast<int32_t>(t)) << 8) + 255 - (h + j);
-              key = kv > key ? kv : key;
-            }
-          }
-        }
-      } else {
-#pragma unroll 4
-        for (int i = i0; i < i0 + cnt; ++i) {
-          const int32_t d = static_cast<int32_t>(dist_int(load(i), wbytes, st.klo, st.khi));
-          ob = __funnelshift_l(static_cast<uint32_t>(thr1 - d), ob, 1);
-          if (kKeepMax<OG>) {
-            const int32_t kv = (d << 8) + 255 - i;
-            key = kv > key ? kv : key;
-          }
-        }
+        for (int j = 0; j < 8; ++j) sample(i + j);
       }
-      ob = cnt > 0 ? __brev(ob) >> (32 - cnt) : 0u;
+#pragma unroll 1
+      for (; i < iend; ++i) sample(i);
+      const uint32_t word = iend > i0 ? __brev(ob) >> (32 - (iend - i0)) : 0u;
 #pragma unroll
-      for (int w = 0; w < NW; ++w) pb[w] = w == blk ? ob : pb[w];
+      for (int w = 0; w < NW; ++w) pb[w] = w == blk ? word : pb[w];
     }
   } else if (KIND == kF32Kind || KIND == kPxKind || (KIND == kAnyKind && S.pair_f32)) {
     // two samples per instruction in float2 lanes, every term on (median - p) / 2: the
@@ -276,68 +248,39 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
       }
       return dq;
     };
+    // the sign of dq - thr4 is 0 exactly when dq >= thr4 (equal: +0; both finite and
+    // non-negative): sign bits of the non-outliers enter at bit 0 and move up
+    uint32_t nb;
+    auto one = [&](float dq, int i) {
+      nb = __funnelshift_l(__float_as_uint(__fsub_rn(dq, thr4)), nb, 1);
+      if (kKeepMax<OG>) {
+        const bool up = dq >= thr4 && dq > dmax;
+        dmax = up ? dq : dmax;
+        imax = up ? i : imax;
+      }
+    };
 #pragma unroll 1
     for (int blk = 0; blk < NW; ++blk) {
-      uint32_t ob = 0u;
       const int i0 = blk * 32, iend = min(n, i0 + 32);
-      if (iend - i0 == 32) {
-        // the sign of dq - thr4 is 0 exactly when dq >= thr4 (equal: +0; both finite and
-        // non-negative): sign bits of non-outliers enter at bit 0 and move up
-        uint32_t nb = 0u;
+      nb = 0u;
+      int i = i0;
 #pragma unroll 1
-        for (int h = i0; h < i0 + 32; h += 16) {
+      for (; i + 8 <= iend; i += 8) {
 #pragma unroll
-          for (int j = 0; j < 16; j += 2) {
-            const int i = h + j;
-            const float2 dq = pair_dist(load(i), load(i + 1));
-            nb = __funnelshift_l(__float_as_uint(__fsub_rn(dq.x, thr4)), nb, 1);
-            nb = __funnelshift_l(__float_as_uint(__fsub_rn(dq.y, thr4)), nb, 1);
-            if (kKeepMax<OG>) {
-              const bool u0 = dq.x >= thr4 && dq.x > dmax;
-              dmax = u0 ? dq.x : dmax;
-              imax = u0 ? i : imax;
-              const bool u1 = dq.y >= thr4 && dq.y > dmax;
-              dmax = u1 ? dq.y : dmax;
-              imax = u1 ? i + 1 : imax;
-            }
-          }
-        }
-        ob = ~__brev(nb);
-      }
-      for (int i = i0; i < iend && iend - i0 < 32; i += 2) {
-        const uint32_t p0 = load(i);
-        const uint32_t p1 = i + 1 < iend ? load(i + 1) : p0;
-        float2 dq = make_float2(0.0f, 0.0f);
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-          if (!((S.wmask >> ch) & 1u)) continue;
-          const uint32_t sel = 0x7604u | (static_cast<uint32_t>(ch) << 4);
-          const float2 nv = make_float2(__uint_as_float(__byte_perm(p0, 0xC6800000u, sel)),
-                                        __uint_as_float(__byte_perm(p1, 0xC6800000u, sel)));
-          const float2 tt = mul2_rn(wq2[ch], add2_rn(mq[ch], nv));
-          const float2 sq = mul2_rn(tt, tt);
-          dq.x = __fadd_rn(dq.x, sq.x);
-          dq.y = __fadd_rn(dq.y, sq.y);
-        }
-        const bool o0 = dq.x >= thr4;
-        ob |= o0 ? (1u << (i & 31)) : 0u;
-        if (kKeepMax<OG>) {
-          const bool up = o0 && dq.x > dmax;
-          dmax = up ? dq.x : dmax;
-          imax = up ? i : imax;
-        }
-        if (i + 1 < iend) {
-          const bool o1 = dq.y >= thr4;
-          ob |= o1 ? (1u << ((i + 1) & 31)) : 0u;
-          if (kKeepMax<OG>) {
-            const bool up = o1 && dq.y > dmax;
-            dmax = up ? dq.y : dmax;
-            imax = up ? i + 1 : imax;
-          }
+        for (int j = 0; j < 8; j += 2) {
+          const float2 dq = pair_dist(load(i + j), load(i + j + 1));
+          one(dq.x, i + j);
+          one(dq.y, i + j + 1);
         }
       }
+#pragma unroll 1
+      for (; i < iend; ++i) {
+        const uint32_t p = load(i);
+        one(pair_dist(p, p).x, i);
+      }
+      const uint32_t word = iend > i0 ? __brev(~nb) >> (32 - (iend - i0)) : 0u;
 #pragma unroll
-      for (int w = 0; w < NW; ++w) pb[w] = w == blk ? ob : pb[w];
+      for (int w = 0; w < NW; ++w) pb[w] = w == blk ? word : pb[w];
     }
     dmax = __fmul_rn(dmax, 4.0f);  // scaled back exactly
   } else {
