@@ -283,7 +283,8 @@ int cp_composite_video_device(cp_ctx* ctx, const uint8_t* const* frames, int32_t
  * first call on a device (with that device current) looks up the array's device address;
  * the address is kept for the life of the process, so a cudaDeviceReset() followed by more
  * calls is not supported. The descriptors are passed to the GPU as kernel parameters, so
- * the call returns without waiting for earlier work on `stream`. All calls share the array:
+ * the call returns without waiting for earlier work on `stream`, reads no host memory after
+ * it returns, and can be captured into a CUDA graph. All calls share the array:
  * calls that overlap on the GPU (other streams, other host threads) race, so order them on
  * one stream. Inputs, outputs and warnings (device array of n_stacks counters, nullable)
  * are as for cp_composite_batch_device. */
