@@ -193,14 +193,15 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
     // flags enter at bit 0 and move up (a funnel shift takes the sign of thr - 1 - d: set
     // iff d >= thr); one bit reversal per word puts sample i at bit i
     uint32_t ob;
+    // extreme: the smallest (thr - 1 - d) * 256 + i is the largest d, earliest sample first
+    // (|thr - 1 - d| < 2^23, i < 256); every D' >= 0 (no integer lies strictly between the
+    // floor and ceiling of a median), so over n >= 1 samples this gives the key's maximum
+    int32_t tmin = 0x7FFFFFFF;
     auto sample = [&](int i) {
       const uint32_t v = load(i) & wbytes;
       const uint32_t t = __dp4a(v, st.khi, __dp4a(v, st.klo, base)) - __dp4a(v, v, 0u);
       ob = __funnelshift_l(t, ob, 1);
-      if (kKeepMax<OG>) {
-        const int32_t kv = ((thr1 - static_cast<int32_t>(t)) << 8) + 255 - i;
-        key = kv > key ? kv : key;
-      }
+      if (kKeepMax<OG>) tmin = min(tmin, static_cast<int32_t>((t << 8) + static_cast<uint32_t>(i)));
     };
 #pragma unroll 1
     for (int blk = 0; blk < NW; ++blk) {
@@ -218,6 +219,7 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
 #pragma unroll
       for (int w = 0; w < NW; ++w) pb[w] = w == blk ? word : pb[w];
     }
+    if (kKeepMax<OG>) key = ((thr1 - (tmin >> 8)) << 8) + 255 - (tmin & 255);
   } else if (KIND == kF32Kind || KIND == kPxKind || (KIND == kAnyKind && S.pair_f32)) {
     // two samples per instruction in float2 lanes, every term on (median - p) / 2: the
     // sample -(2^14 + p/2) is one byte permute of the pixel byte into -2^14's mantissa, the
@@ -251,10 +253,12 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
     // the sign of dq - thr4 is 0 exactly when dq >= thr4 (equal: +0; both finite and
     // non-negative): sign bits of the non-outliers enter at bit 0 and move up
     uint32_t nb;
+    // extreme: the largest distance of all samples, earliest first. With an outlier it is an
+    // outlier's (the largest is >= every outlier's >= thr4); without one it is not used.
     auto one = [&](float dq, int i) {
       nb = __funnelshift_l(__float_as_uint(__fsub_rn(dq, thr4)), nb, 1);
       if (kKeepMax<OG>) {
-        const bool up = dq >= thr4 && dq > dmax;
+        const bool up = dq > dmax;
         dmax = up ? dq : dmax;
         imax = up ? i : imax;
       }
