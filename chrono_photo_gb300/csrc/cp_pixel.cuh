@@ -58,6 +58,33 @@ DEVI PxStat<C> px_stat(const StackDev& S, uint32_t lo3, uint32_t hi3, const floa
 // mask keeps them out of the selections), so the loads need no bound test.
 template <int C, int NW, typename Load>
 DEVI void pixel_planes(Load load, uint32_t (&P)[C][8][NW]) {
+  if constexpr (C == 3) {
+    // RGB: the 12 channel bytes of 4 groups' words r are first packed into 3 words (byte
+    // lanes (g0c0 g0c1 g0c2 g1c0), (g1c1 g1c2 g2c0 g2c1), (g2c2 g3c0 g3c1 g3c2)), so 3 bit
+    // transposes do the work of 4 with no lane spent on the unused fourth byte
+#pragma unroll
+    for (int blk = 0; blk < NW; ++blk) {
+      uint32_t x[3][8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const uint32_t a0 = load(blk * 32 + r), a1 = load(blk * 32 + 8 + r);
+        const uint32_t a2 = load(blk * 32 + 16 + r), a3 = load(blk * 32 + 24 + r);
+        x[0][r] = __byte_perm(a0, a1, 0x4210);
+        x[1][r] = __byte_perm(a1, a2, 0x5421);
+        x[2][r] = __byte_perm(a2, a3, 0x6542);
+      }
+      transpose8(x[0]);
+      transpose8(x[1]);
+      transpose8(x[2]);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {  // plane word: groups 0..3 of the channel in bytes 0..3
+        P[0][r][blk] = __byte_perm(__byte_perm(x[0][r], x[1][r], 0x0630), x[2][r], 0x5210);
+        P[1 % C][r][blk] = __byte_perm(__byte_perm(x[0][r], x[1][r], 0x0741), x[2][r], 0x6210);
+        P[2 % C][r][blk] = __byte_perm(__byte_perm(x[0][r], x[1][r], 0x0052), x[2][r], 0x7410);
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int blk = 0; blk < NW; ++blk) {
     uint32_t a[4][8];
