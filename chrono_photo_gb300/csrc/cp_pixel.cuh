@@ -350,15 +350,22 @@ DEVI uint32_t px_simple(const StackDev& S, int n, Load load) {
 #pragma unroll
     for (int ch = 0; ch < C; ++ch)
       if ((S.wmask >> ch) & 1u) ones |= 1u << (8 * ch);
-    int32_t ext = darker ? 0x7FFFFFFF : -1;
-    for (int i = 0; i < n; ++i) {
-      const uint32_t px = load(i) & (0xFFFFFFFFu >> (32 - 8 * C));
-      const int32_t v = static_cast<int32_t>(__dp4a(px, ones, 0u));
-      const bool up = darker ? (v < ext) : (v > ext);
-      ext = up ? v : ext;
-      outw = up ? px : outw;
+    // key v * 128 + i (darker: smallest) or v * 128 + 127 - i (lighter: largest) of the
+    // channel sum v <= 1020 and sample i < 128: the extreme, earliest sample first; the
+    // winning sample is loaded once at the end
+    int idx;
+    if (darker) {
+      int32_t key = 0x7FFFFFFF;
+      for (int i = 0; i < n; ++i)
+        key = min(key, static_cast<int32_t>(__dp4a(load(i), ones, 0u)) * 128 + i);
+      idx = key & 127;
+    } else {
+      int32_t key = -1;
+      for (int i = 0; i < n; ++i)
+        key = max(key, static_cast<int32_t>(__dp4a(load(i), ones, 0u)) * 128 + 127 - i);
+      idx = 127 - (key & 127);
     }
-    return outw;
+    return load(idx) & (0xFFFFFFFFu >> (32 - 8 * C));
   }
   float ext = darker ? FLT_MAX : -FLT_MAX;
   for (int i = 0; i < n; ++i) {
@@ -383,17 +390,16 @@ DEVI void px_simple_pair(const StackDev& S, int n, Load load, uint32_t& dark, ui
 #pragma unroll
   for (int ch = 0; ch < C; ++ch)
     if ((S.wmask >> ch) & 1u) ones |= 1u << (8 * ch);
-  int32_t lo = 0x7FFFFFFF, hi = -1;
-  dark = light = 0u;
+  // keys as in px_simple: the smallest v * 128 + i is the darkest sample and the largest
+  // v * 128 + 127 - i the lightest, earliest first (dp4a with `ones` ignores bytes >= C)
+  int32_t kd = 0x7FFFFFFF, kl = -1;
   for (int i = 0; i < n; ++i) {
-    const uint32_t px = load(i) & (0xFFFFFFFFu >> (32 - 8 * C));
-    const int32_t v = static_cast<int32_t>(__dp4a(px, ones, 0u));
-    const bool dn = v < lo, up = v > hi;
-    lo = dn ? v : lo;
-    dark = dn ? px : dark;
-    hi = up ? v : hi;
-    light = up ? px : light;
+    const int32_t v = static_cast<int32_t>(__dp4a(load(i), ones, 0u));
+    kd = min(kd, v * 128 + i);
+    kl = max(kl, v * 128 + 127 - i);
   }
+  dark = load(kd & 127) & (0xFFFFFFFFu >> (32 - 8 * C));
+  light = load(127 - (kl & 127)) & (0xFFFFFFFFu >> (32 - 8 * C));
 }
 
 struct PxOut {
