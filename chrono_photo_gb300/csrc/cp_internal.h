@@ -88,7 +88,8 @@ struct StackDev {
   uint32_t sample_mask[4];  // frames in the (sub)sample, bit i of word i/32
   uint64_t seed;
   int64_t wait_cycles;  // SM clock cycles before a bounded wait gives up
-  uint64_t pad0;        // keeps the descriptor a multiple of 16 bytes (copied in 16-byte words)
+  uint32_t unit_fade;   // every fade factor is exactly 1 (the epilogue skips its fade lookups)
+  uint32_t pad0;        // keeps the descriptor a multiple of 16 bytes (copied in 16-byte words)
   // per-frame tables
   const uint8_t* frames[CP_MAX_FRAMES];
   int32_t crop[2 * CP_MAX_FRAMES];

@@ -420,6 +420,13 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
   PxOut r;
   auto load = [&](int i) -> uint32_t { return load_raw(i) & (0xFFFFFFFFu >> (32 - 8 * C)); };
   const bool fast = KIND == kIntKind || ((KIND == kAnyKind || KIND == kPxKind) && S.fast_int);
+  // fade factor of sample i; without a fade every factor is 1 (and x * 1 = x exactly), so
+  // the per-lane lookups (a different sample in each lane) are skipped
+  auto fade_at = [&](int i) -> float {
+    float f = 1.0f;
+    if (!S.unit_fade) f = S.fade[i];
+    return f;
+  };
   auto dsq_px = [&](uint32_t px) -> float {  // dist_sq of a sample, recomputed
     if (fast)
       return static_cast<float>(dist_int(px, wbytes, st.klo, st.khi)) +
@@ -560,7 +567,7 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
     }
     const uint32_t sample = load(si);
     if (!extreme) dsq = dsq_px(sample);
-    blend = nout == 0 ? 0.0f : __fmul_rn(S.fade[si], blend_value(S, __fsqrt_rn(dsq)));
+    blend = nout == 0 ? 0.0f : __fmul_rn(fade_at(si), blend_value(S, __fsqrt_rn(dsq)));
     pix = blend_into_u8<C>(pix, sample, blend);
     mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));
     chosen = nout == 0 ? -1 : si;
@@ -571,7 +578,7 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
     float binv = 1.0f;
     auto blend_one = [&](int f) {
       const uint32_t sv = load(f);
-      const float bk = __fmul_rn(S.fade[f], blend_value(S, __fsqrt_rn(dsq_px(sv))));
+      const float bk = __fmul_rn(fade_at(f), blend_value(S, __fsqrt_rn(dsq_px(sv))));
       // blend_into_f32_u8, src/color.rs:32-44
       if (bk <= 0.0f) {
       } else if (bk >= 1.0f) {
@@ -665,7 +672,7 @@ DEVI PxOut px_epilogue(const StackDev& S, int n, const PxStat<C>& st, uint32_t w
     // the fade of an averaged outlier is taken at sample 0 (src/chrono.rs:467), that of a
     // single one at its own sample; no outlier: no blend (the sums divided by 0 are unused)
     const float bk =
-        __fmul_rn(S.fade[nout == 1 ? si : 0], blend_value(S, __fdiv_rn(mdist, kf)));
+        __fmul_rn(fade_at(nout == 1 ? si : 0), blend_value(S, __fdiv_rn(mdist, kf)));
     blend = nout == 0 ? 0.0f : bk;
     pix = blend_into_u8<C>(pix, sample, blend);
     mask = sat_u8(rround(__fmul_rn(blend, 255.0f)));

@@ -250,8 +250,11 @@ int prepare_stack(cp_ctx* ctx, const cp_stack* st, const cp_params* p,
     return CP_ERR_ARG;
   }
   d->no_fade = 1u;
-  for (int i = 0; i < n; ++i)
+  d->unit_fade = 1u;
+  for (int i = 0; i < n; ++i) {
     if (!(d->fade[i] >= 1.0f)) d->no_fade = 0u;
+    if (d->fade[i] != 1.0f) d->unit_fade = 0u;
+  }
   return CP_OK;
 }
 
