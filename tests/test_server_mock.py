@@ -314,13 +314,18 @@ def test_device_wait_that_gave_up_fails_exactly_its_launch(dev):
     a1, a2 = srv.submit(frames_for(4, seed=1))[1], srv.submit(frames_for(4, seed=2))[1]
     assert poll(lambda: stats(dev)["uploads"] == 8)
     dev.mock_fail_launch_words(1)
-    dev.mock_hold(HOLD_KERNELS)  # both jobs' uploads land together: one launch
-    assert poll(lambda: stats(dev)["launches"] == 1)
+    dev.mock_hold(HOLD_KERNELS)  # both uploads land; the jobs go out in one or two launches
+    assert poll(lambda: stats(dev)["launches"] >= 1)
     dev.mock_hold(0)
+    status = []
     for jid in (a1, a2):
         rc, res, _, _ = srv.wait(jid)
-        assert rc == _abi.CP_OK and res.status == _abi.CP_ERR_TIMEOUT
-    assert stats(dev)["max_stacks"] == 2
+        assert rc == _abi.CP_OK
+        status.append(res.status)
+    if stats(dev)["max_stacks"] == 2:  # one launch: both jobs read its error word
+        assert status == [_abi.CP_ERR_TIMEOUT] * 2
+    else:  # the first launch had the word set, the second a clear one
+        assert sorted(status) == sorted([_abi.CP_ERR_TIMEOUT, _abi.CP_OK])
     srv.check_ok(srv.submit(frames_for(4, seed=3))[1])  # the next launch has a clear word
     assert_clean(dev, srv.close()[1])
 
