@@ -206,3 +206,25 @@ def test_darker_lighter_pair(ctx, order):
         ref = device_single(ctx, frames, p)
         assert np.array_equal(o, ref[0]), kw
         cases.assert_close_u8(o, oracle.composite(frames, p)[0], what=str(kw))
+
+
+def test_multi_paired_distances_with_a_weight_zero_channel(ctx):
+    """Paired-f32 settings with a weight-0 channel in one multi-setting launch: each equals
+    its single-setting result and the oracle."""
+    rng = np.random.default_rng(41)
+    frames = cases.random_stack(rng, 64, 24, 80, 3, n_spots=6)
+    kws = [dict(mode="outlier", threshold="rel/3/6", outlier="extreme", background="first",
+                weights=[1, 0, 1, 1]),
+           dict(mode="outlier", threshold="abs/0.05/0.2", outlier="average", background="first",
+                weights=[0.5, 0, 2.0, 1]),
+           dict(mode="outlier", threshold="abs/0.05/0.2", outlier="forward", background="first",
+                weights=[0.5, 0, 2.0, 1])]
+    ps = [cases.params(**kw) for kw in kws]
+    got = device_multi(ctx, frames, ps)
+    for kw, p, (o, b, wn) in zip(kws, ps, got):
+        ref = device_single(ctx, frames, p)
+        assert np.array_equal(o, ref[0]) and np.array_equal(b, ref[1]) and wn == ref[2], kw
+        orc = oracle.composite(frames, p)
+        cases.assert_close_u8(o, orc[0], what="composite %s" % kw["threshold"])
+        cases.assert_close_u8(b, orc[1], what="blend %s" % kw["threshold"])
+        assert wn == orc[2]

@@ -284,3 +284,16 @@ def test_processors_take_png_paths(ctx, small, tmp_path):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     sp = cg_api.SimpleProcessor(darker=False, context=ctx)
     assert np.array_equal(sp.process(small), sp.process(paths))
+
+
+@pytest.mark.parametrize("thr,weights", [("rel/3/6", [1, 0, 1, 1]), ("rel/2/5", [0.5, 2.0, 0, 1]),
+                                         ("abs/0.05/0.2", [0.5, 0, 2.0, 1])])
+def test_paired_distances_with_a_weight_zero_channel(ctx, thr, weights):
+    """Paired-f32 distances (rel thresholds, or abs with weights other than 0/1) where one
+    channel has weight 0: that channel adds +0 to every distance, as the reference's skipped
+    term does (src/chrono.rs:261-279), including a word of 32 samples and a partial one."""
+    rng = np.random.default_rng(31)
+    frames = cases.random_stack(rng, 45, 16, 48, 3, n_spots=6)
+    for outlier in ("extreme", "average", "forward"):
+        compare(ctx, frames, mode="outlier", threshold=thr, outlier=outlier, background="first",
+                weights=weights)
