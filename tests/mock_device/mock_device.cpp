@@ -690,6 +690,31 @@ void mock_set_pool_limit(uint64_t bytes) {
   s.pool_limit = bytes;
 }
 
+// prepare_stack's derived descriptor fields for a stack and its options (frames at dummy
+// device addresses), for host-only tests of the option semantics. ints: n, nw, n_sub, med_k,
+// med_pair, q1_k, q1_pair, q3_k, q3_pair, fast_int, pair_f32, no_fade, unit_fade, wmask,
+// thr_abs, thr_int[0..4] (20 values); floats: q1_frac, q3_frac, thr_min, thr_max, thr_scale,
+// thr_sq, then fade[0..n-1]. Returns prepare_stack's status.
+int mock_prepare(const cp_stack* st, const cp_params* p, int32_t* ints, float* floats) {
+  if (!st || st->n < 1 || st->n > CP_MAX_FRAMES) return CP_ERR_ARG;
+  std::vector<const uint8_t*> fr(static_cast<size_t>(st->n),
+                                 reinterpret_cast<const uint8_t*>(uintptr_t(256)));
+  StackDev d;
+  const int rc = cp::prepare_stack(nullptr, st, p, fr.data(), &d);
+  if (rc) return rc;
+  const int32_t iv[] = {d.n, d.nw, d.n_sub, d.med_k, d.med_pair, d.q1_k, d.q1_pair, d.q3_k,
+                        d.q3_pair, static_cast<int32_t>(d.fast_int),
+                        static_cast<int32_t>(d.pair_f32), static_cast<int32_t>(d.no_fade),
+                        static_cast<int32_t>(d.unit_fade), static_cast<int32_t>(d.wmask),
+                        d.thr_abs, d.thr_int[0], d.thr_int[1], d.thr_int[2], d.thr_int[3],
+                        d.thr_int[4]};
+  std::memcpy(ints, iv, sizeof iv);
+  const float fv[] = {d.q1_frac, d.q3_frac, d.thr_min, d.thr_max, d.thr_scale, d.thr_sq};
+  std::memcpy(floats, fv, sizeof fv);
+  for (int i = 0; i < d.n; ++i) floats[6 + i] = d.fade[i];
+  return CP_OK;
+}
+
 // Copies up to n counters (the Stat order) into out; returns how many there are.
 int mock_stats(uint64_t* out, int n) {
   State& s = S();

@@ -15,9 +15,6 @@ first error (src/main.rs:22-211); the server keeps that per-output result, and a
 job (a failed allocation, a device-side wait that gave up) fails that job only.
 """
 import ctypes as ct
-import os
-import shutil
-import subprocess
 import threading
 import time
 
@@ -25,12 +22,6 @@ import numpy as np
 import pytest
 
 from chrono_photo_gb300 import _abi
-
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CSRC = os.path.join(ROOT, "chrono_photo_gb300", "csrc")
-MOCK = os.path.join(ROOT, "tests", "mock_device")
-SOURCES = [os.path.join(CSRC, f) for f in ("cp_server.cpp", "cp_prepare.cpp", "cp_memory.cpp")]
-SOURCES.append(os.path.join(MOCK, "mock_device.cpp"))
 
 STATS = ("uploads", "upload_bytes", "downloads", "launches", "launches_run", "live_events",
          "live_streams", "live_pools", "pool_bytes", "live_host", "live_dev", "misuse",
@@ -42,37 +33,8 @@ P, U64, I32 = ct.c_void_p, ct.c_uint64, ct.c_int32
 
 
 @pytest.fixture(scope="module")
-def mock(tmp_path_factory):
-    gxx = shutil.which("g++")
-    if gxx is None:
-        pytest.skip("g++ not found")
-    out = str(tmp_path_factory.mktemp("mock_device") / "libserver_mock.so")
-    # -Bsymbolic: the library's own runtime functions win over a CUDA runtime that another
-    # module (torch) has already loaded into the process with global symbols
-    subprocess.run([gxx, "-std=c++17", "-O1", "-g", "-fPIC", "-shared", "-pthread", "-Wall",
-                    "-Wl,-Bsymbolic", "-I", MOCK, "-o", out] + SOURCES, check=True)
-    lib = ct.CDLL(out)
-    for name, res, args in (
-            ("mock_ctx_create", P, [U64]), ("mock_ctx_destroy", None, [P]),
-            ("mock_ctx_used", U64, [P]), ("mock_ctx_launches", U64, [P]),
-            ("mock_reset", None, []), ("mock_shutdown", None, []),
-            ("mock_hold", None, [ct.c_uint]), ("mock_fail_launch_words", None, [ct.c_int]),
-            ("mock_fault_launches", None, [ct.c_int]),
-            ("mock_fail_allocs", None, [ct.c_uint, ct.c_int]),
-            ("mock_set_pool_limit", None, [U64]),
-            ("mock_stats", ct.c_int, [ct.POINTER(U64), ct.c_int]),
-            ("mock_wait_idle", ct.c_int, [ct.c_int]),
-            ("cp_server_create", ct.c_int, [P, U64, I32, ct.POINTER(P)]),
-            ("cp_server_submit", ct.c_int, [P, ct.POINTER(_abi.Job), ct.POINTER(U64)]),
-            ("cp_server_wait", ct.c_int, [P, U64, I32, ct.POINTER(_abi.JobResult)]),
-            ("cp_server_cancel", ct.c_int, [P, U64]),
-            ("cp_server_destroy", ct.c_int, [P]),
-            ("cp_params_default", None, [ct.POINTER(_abi.Params)]),
-            ("cp_ctx_fail_allocations", ct.c_int, [P, I32]),
-            ("cp_ctx_last_error", ct.c_int, [P, ct.c_char_p, ct.c_size_t])):
-        fn = getattr(lib, name)
-        fn.restype = res
-        fn.argtypes = args
+def mock(mock_device_lib):
+    lib = mock_device_lib
     yield lib
     lib.mock_shutdown()
 
