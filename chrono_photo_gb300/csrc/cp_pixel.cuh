@@ -201,7 +201,7 @@ constexpr bool kKeepMax = OG == kOgAny || OG == kOgSingle;
 
 // Distance pass over samples 0..n-1 (src/chrono.rs:257-288): outlier flags pb (bit i of word
 // i/32), and for `extreme` the largest distance, earliest sample first: integer kind as the
-// key (D' << 8) + 255 - i (key < 0: none), f32 kinds as (dmax, imax).
+// key (D' << 8) + 255 - i, f32 kinds as (dmax, imax).
 template <int C, int NW, int KIND, int OG, typename Load>
 DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wbytes, Load load,
                       uint32_t (&pb)[NW], int32_t& key, float& dmax, int& imax) {
@@ -221,8 +221,11 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
     // iff d >= thr); one bit reversal per word puts sample i at bit i
     uint32_t ob;
     // extreme: the smallest (thr - 1 - d) * 256 + i is the largest d, earliest sample first
-    // (|thr - 1 - d| < 2^23, i < 256); every D' >= 0 (no integer lies strictly between the
-    // floor and ceiling of a median), so over n >= 1 samples this gives the key's maximum
+    // (i < 256); every D' >= 0 (no integer lies strictly between the floor and ceiling of a
+    // median), so over n >= 1 samples this gives the key's maximum. With any outlier,
+    // thr <= 3 * 255^2 and |thr - 1 - d| < 2^19, so the product is exact; with none (a
+    // threshold beyond every distance) it may wrap, and only its index bits, a valid sample,
+    // are read
     int32_t tmin = 0x7FFFFFFF;
     auto sample = [&](int i) {
       const uint32_t v = load(i) & wbytes;
