@@ -177,7 +177,8 @@ def test_sample_subset(ctx):
             background="median", sample=list(range(1, 40, 3)))
 
 
-@pytest.mark.parametrize("thr", ["abs/0/0.1", "abs/1/1", "abs/0.02", "rel/0/1", "rel/0.5"])
+@pytest.mark.parametrize("thr", ["abs/0/0.1", "abs/1/1", "abs/0.02", "rel/0/1", "rel/0.5",
+                                 "abs/30/40"])
 def test_threshold_edges(ctx, thr):
     rng = np.random.default_rng(21)
     frames = cases.random_stack(rng, 9, 16, 16, 3)
