@@ -202,7 +202,9 @@ constexpr bool kKeepMax = OG == kOgAny || OG == kOgSingle;
 // Distance pass over samples 0..n-1 (src/chrono.rs:257-288): outlier flags pb (bit i of word
 // i/32), and for `extreme` the largest distance, earliest sample first: integer kind as the
 // key (D' << 8) + 255 - i, f32 kinds as (dmax, imax).
-template <int C, int NW, int KIND, int OG, typename Load>
+// CH: samples per straight-line chunk of the integer pass (8 keeps the code small for the
+// kernels that walk many code paths per tile; the sliding-window kernel takes whole words).
+template <int C, int NW, int KIND, int OG, typename Load, int CH = 8>
 DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wbytes, Load load,
                       uint32_t (&pb)[NW], int32_t& key, float& dmax, int& imax) {
   key = st.nh > 0 ? -1 : 255;
@@ -239,9 +241,9 @@ DEVI void px_distance(const StackDev& S, int n, const PxStat<C>& st, uint32_t wb
       ob = 0u;
       int i = i0;
 #pragma unroll 1
-      for (; i + 8 <= iend; i += 8) {
+      for (; i + CH <= iend; i += CH) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) sample(i + j);
+        for (int j = 0; j < CH; ++j) sample(i + j);
       }
 #pragma unroll 1
       for (; i < iend; ++i) sample(i);

@@ -164,7 +164,8 @@ __global__ void __launch_bounds__(32, 16) k_video_slide(const __grid_constant__ 
       int32_t key;
       float dmax;
       int imax;
-      px_distance<C, NW, kIntKind, OG>(S, n, st, wbytes, load, pb, key, dmax, imax);
+      px_distance<C, NW, kIntKind, OG, decltype(load), 32>(S, n, st, wbytes, load, pb, key, dmax,
+                                                         imax);
       const PxOut r = px_epilogue<C, NW, kIntKind, OG, BG>(S, n, st, wbytes, pb, key, dmax,
                                                            imax, px0 + lane, sum, load);
       // stage the composite and mask bytes, then store the rows coalesced
